@@ -1,0 +1,190 @@
+/*
+ * logo_gpu.h -- C ABI of the GB300 (sm_103a) 2-opt local-search engine.
+ *
+ * Drop-in for the 2-opt hot path of the LOGO TSP solver (krocki/
+ * LOGO-TSP-Solver v0.62).  The reference reaches its CUDA backend through the
+ * C++ LocalSolver interface (src/solvers/localSolver.h:25-132) and calls the
+ * CUDA runtime directly from CUDASolver (src/solvers/CUDASolver.cpp); this
+ * header is the plain-C boundary that replaces that backend.  No torch or
+ * CUDA types appear in the signatures: coordinates, routes and results are
+ * host arrays owned by the caller, and every call returns a logo_status
+ * (the reference prints and exit(-1)s instead, src/utils/UtilsCUDA.cpp:318-328).
+ *
+ * Arithmetic contract.  Distances are the reference's per-edge EUC_2D nint
+ * (int)(sqrtf(dx*dx + dy*dy) + 0.5f)   (src/cuda/cuda_common.h:33-40,
+ * src/headers.h:126-133) evaluated in IEEE binary32 without FMA contraction
+ * and with a correctly rounded sqrt.  Moves are chosen best-improvement over
+ * tour positions 1 <= i < j <= n-2 with the lowest-(i, j) tie rule of the
+ * reference CPU solver (src/solvers/cpuSolver.cpp:188-230) and applied as
+ * rotate-then-reverse (src/solvers/twoOptLocalSolver.cpp:41-48), so every
+ * move, tour and length is bit-identical to the reference CPU path with that
+ * distance.
+ *
+ * Limits.  3 <= n <= LOGO_MAX_CITIES; all coordinates finite; the bounding
+ * box diagonal of the coordinates below LOGO_MAX_DIAGONAL (the packed argmin
+ * key stores delta in 22 bits).
+ *
+ * Threading.  A logo_ctx belongs to one host thread at a time; it owns one
+ * CUDA stream on its device.  Different contexts may be used concurrently.
+ */
+#ifndef LOGO_GPU_H
+#define LOGO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LOGO_MAX_CITIES 2097152u   /* MAX_CITIES, src/defs.h:25 */
+#define LOGO_MAX_DIAGONAL 2000000.0
+
+typedef enum logo_status {
+    LOGO_OK = 0,
+    LOGO_ERR_INVALID_ARG = 1,  /* bad pointer, size, route or coordinates */
+    LOGO_ERR_OOM = 2,          /* device or pinned-host allocation failed */
+    LOGO_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    LOGO_ERR_TIMEOUT = 4,      /* a bounded device-side wait ran out */
+    LOGO_ERR_DEVICE_FAULT = 5, /* the device status word reports an error */
+    LOGO_ERR_MOVE_LIMIT = 6,   /* a descent reached its max_moves */
+    LOGO_ERR_NO_DEVICE = 7,    /* no usable CUDA device */
+    LOGO_ERR_BUSY = 8,         /* server queue full / slot unavailable */
+    LOGO_ERR_NOT_FOUND = 9     /* unknown request id */
+} logo_status;
+
+/* city_coords, src/defs.h:173-178 */
+typedef struct logo_xy {
+    float x;
+    float y;
+} logo_xy;
+
+/* best2_out, src/defs.h:181-187: the reported move (i, j) deletes tour edges
+ * (i-1, i) and (j-1, j); minchange < 0, or 0 with i = j = 0 when no
+ * improving move exists. */
+typedef struct logo_move {
+    uint32_t i;
+    uint32_t j;
+    int32_t minchange;
+} logo_move;
+
+typedef struct logo_stats {
+    uint64_t moves;        /* 2-opt moves applied */
+    uint64_t sweeps;       /* best-improvement sweeps evaluated */
+    uint64_t pair_evals;   /* sweeps * (n-2)(n-3)/2 */
+    uint64_t descents;     /* local-search descents run */
+    uint64_t kicks;        /* perturbations applied */
+    uint64_t accepted;     /* descents that improved the best tour */
+    uint64_t start_length; /* length of the input tour */
+    uint64_t final_length; /* length of the returned tour */
+    double device_ms;      /* device time of the call (CUDA events) */
+} logo_stats;
+
+/* ILS perturbation kinds. */
+#define LOGO_KICK_SEGMENT 0       /* reference kick: random segment reversal,
+                                     src/solvers/ILSGlobalSolver.cpp:37-48 */
+#define LOGO_KICK_DOUBLE_BRIDGE 1 /* double bridge with 3 uniform cuts
+                                     (no reference counterpart) */
+
+typedef struct logo_ctx logo_ctx;
+
+/* ---- single instance ------------------------------------------------------ */
+
+/* Creates a context for one instance on `device` and copies the coordinates
+ * to it.  Replaces CUDASolver::init (src/solvers/CUDASolver.cpp:52-139). */
+logo_status logo_ctx_create(int device, const logo_xy *coords, uint32_t n,
+                            logo_ctx **out);
+
+/* Frees the context.  Replaces CUDASolver::cleanCUDA
+ * (src/solvers/CUDASolver.cpp:386-400).  NULL is accepted. */
+logo_status logo_ctx_destroy(logo_ctx *ctx);
+
+/* Text of the last error on this context (sticky until the next failing
+ * call), or of the last failed logo_ctx_create on this thread when ctx is
+ * NULL.  Never NULL. */
+const char *logo_last_error(const logo_ctx *ctx);
+
+/* One best-improvement sweep over `route` (n city ids): the best 2-opt move
+ * or minchange = 0.  Replaces LocalSolver::optimizeStep / CUDASolver::
+ * optimizeStep (src/solvers/localSolver.h:124-125,
+ * src/solvers/CUDASolver.cpp:285-386). */
+logo_status logo_best_move(logo_ctx *ctx, const uint32_t *route, logo_move *out);
+
+/* 2-opt descent to a local optimum; route_inout is overwritten (on success
+ * only) with the final tour.  max_moves = 0 means no limit.  Replaces
+ * TwoOptLocalSolver::optimize (src/solvers/twoOptLocalSolver.cpp:22-64). */
+logo_status logo_descend(logo_ctx *ctx, uint32_t *route_inout, uint64_t max_moves,
+                         logo_stats *stats);
+
+/* Iterated local search: descend, then `kicks` times {kick; descend; keep
+ * the tour if strictly shorter than the best, else return to the best}.
+ * route_inout receives the best tour.  Replaces
+ * ILSGlobalSolverSequential::optimize
+ * (src/solvers/ILSGlobalSolverSequential.cpp:60-100), whose stop rule needs
+ * a known optimum, with an explicit kick count; kicks draw from SplitMix64
+ * seeded with `seed` instead of rand(). */
+logo_status logo_ils(logo_ctx *ctx, uint32_t *route_inout, uint32_t kicks,
+                     uint64_t seed, int kick_kind, logo_stats *stats);
+
+/* Tour length (routeLength, src/headers.h:170-189). */
+logo_status logo_tour_length(logo_ctx *ctx, const uint32_t *route, uint64_t *length);
+
+/* logo_descend that also records every applied move as (minchange, i, j)
+ * int32 triples into trace[0 .. 3*trace_cap) -- the per-move report that
+ * TwoOptLocalSolver::optimize prints when showLocalOptimizationInfo is set
+ * (src/solvers/twoOptLocalSolver.cpp:56-65). */
+logo_status logo_descend_trace(logo_ctx *ctx, uint32_t *route_inout, uint64_t max_moves,
+                               int32_t *trace, uint64_t trace_cap, logo_stats *stats);
+
+/* ---- resident tour (no host copies between calls) --------------------------- */
+
+/* Uploads a start tour that stays on the device. */
+logo_status logo_set_route(logo_ctx *ctx, const uint32_t *route);
+/* Downloads the resident tour. */
+logo_status logo_get_route(logo_ctx *ctx, uint32_t *route);
+/* Runs up to max_moves descent moves on the resident tour; stats->moves
+ * receives how many were applied (fewer means a local optimum was reached). */
+logo_status logo_descend_resident(logo_ctx *ctx, uint64_t max_moves, logo_stats *stats);
+/* One sweep on the resident tour without applying the move. */
+logo_status logo_sweep_resident(logo_ctx *ctx, logo_move *out);
+/* Length of the resident tour. */
+logo_status logo_length_resident(logo_ctx *ctx, uint64_t *length);
+/* Waits for the context's stream. */
+logo_status logo_sync(logo_ctx *ctx);
+
+/* ---- introspection ------------------------------------------------------------- */
+
+typedef struct logo_ctx_info {
+    uint32_t n;
+    int device;
+    int rows_per_thread;  /* sweep tile shape chosen for this n */
+    int warps_per_cta;
+    uint32_t tile_cols;
+    uint32_t tiles;       /* CTAs per sweep */
+    float filter_margin;  /* bound on |exact - approximate delta| */
+    uint32_t graph_steps; /* sweep+apply steps per graph launch */
+} logo_ctx_info;
+
+logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
+
+/* Overrides the sweep tile shape (rows per thread, warps per CTA, columns per
+ * tile); used by the autotuner.  Invalid shapes return INVALID_ARG. */
+logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per_cta,
+                               uint32_t tile_cols);
+
+/* The CUDA stream (cudaStream_t) the context launches on, for callers that
+ * time or order work against it. */
+void *logo_ctx_stream(logo_ctx *ctx);
+
+/* Library version string. */
+const char *logo_version(void);
+
+/* Self-check of the sweep's exactness argument: the largest relative error of
+ * the device's approximate square root over every positive normal binary32
+ * input, against the correctly rounded root.  The sweep's filter margin
+ * assumes it is at most 2^-20.  No reference counterpart. */
+logo_status logo_diag_sqrt_error(int device, double *max_rel_err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LOGO_GPU_H */

@@ -1,0 +1,660 @@
+// C ABI of the single-instance engine (include/logo_gpu.h).
+//
+// Host side of the path the reference runs in CUDASolver + TwoOptLocalSolver +
+// ILSGlobalSolverSequential.  The reference crosses the host/device boundary
+// three times per move (gather + H2D of the ordered coordinates, launch, D2H
+// of best2_out; src/solvers/CUDASolver.cpp:285-386) and applies the move and
+// measures the tour on the host (twoOptLocalSolver.cpp:41-50).  Here the tour
+// stays in HBM: a descent is a CUDA graph of `graph_steps` (sweep, apply)
+// pairs replayed until the device-side convergence flag is set; the host
+// reads one small status block per replay.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/logo_gpu.h"
+#include "logo_device.cuh"
+#include "logo_internal.h"
+
+using namespace logo;
+
+struct logo_ctx {
+    int device = 0;
+    uint32_t n = 0;
+    cudaStream_t stream = nullptr;
+    float2* d_xy = nullptr;
+    OrderedCity* d_Q[2] = {nullptr, nullptr};
+    uint32_t* d_route[2] = {nullptr, nullptr};
+    OrderedCity* d_Qbest = nullptr;
+    uint32_t* d_route_best = nullptr;
+    DevState* d_st = nullptr;
+    DevState* h_st = nullptr;  // pinned mirror
+    uint32_t* h_route = nullptr;  // pinned staging
+    uint2* d_tiles = nullptr;
+    uint32_t ntiles = 0;
+    int R = 8, NW = 4;
+    uint32_t cb = 1024;
+    float margin = 0.f;
+    double diag = 0.0;
+    cudaGraphExec_t chunk_exec = nullptr;
+    uint32_t chunk_steps = 8;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool have_route = false;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_create_err;
+
+const char* kVersion = "logo-gb300 0.1 (sm_103a)";
+
+logo_status fail(logo_ctx* c, logo_status s, const std::string& msg) {
+    if (c)
+        c->err = msg;
+    else
+        g_create_err = msg;
+    return s;
+}
+
+#define CK(ctx, call)                                                              \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? LOGO_ERR_OOM         \
+                                                             : LOGO_ERR_CUDA,      \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+TourBufs bufs(const logo_ctx* c) {
+    TourBufs T;
+    T.Q[0] = c->d_Q[0];
+    T.Q[1] = c->d_Q[1];
+    T.route[0] = c->d_route[0];
+    T.route[1] = c->d_route[1];
+    T.Qbest = c->d_Qbest;
+    T.route_best = c->d_route_best;
+    T.xy = c->d_xy;
+    T.n = c->n;
+    T.st = c->d_st;
+    return T;
+}
+
+SweepLaunch sweep_args(const logo_ctx* c) {
+    SweepLaunch L;
+    L.Q0 = c->d_Q[0];
+    L.Q1 = c->d_Q[1];
+    L.n = c->n;
+    L.tiles = c->d_tiles;
+    L.ntiles = c->ntiles;
+    L.cb = c->cb;
+    L.R = c->R;
+    L.NW = c->NW;
+    L.margin = c->margin;
+    L.st = c->d_st;
+    return L;
+}
+
+uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) / 2; }
+
+// Default tile shape by size (overridable through logo_ctx_set_shape).
+void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb) {
+    if (n >= 40000) {
+        R = 8; NW = 4; cb = 1024;
+    } else if (n >= 12000) {
+        R = 8; NW = 4; cb = 256;
+    } else if (n >= 3000) {
+        R = 4; NW = 4; cb = 128;
+    } else {
+        R = 2; NW = 2; cb = 64;
+    }
+}
+
+// Tiles of the pair triangle: rows [row0, row0 + NW*32*R) x columns
+// [col0, col0 + cb); full tiles first, diagonal tiles last.
+std::vector<uint2> make_tiles(uint32_t n, int R, int NW, uint32_t cb) {
+    std::vector<uint2> full, diag;
+    if (n < 5) return full;
+    const uint32_t rt = (uint32_t)(NW * 32 * R);
+    for (uint32_t row0 = 1; row0 + 3 <= n; row0 += rt) {
+        const uint32_t row_last = std::min(row0 + rt - 1, n - 3);
+        for (uint32_t col0 = row0 + 2; col0 <= n - 1; col0 += cb) {
+            uint2 t = make_uint2(row0, col0);
+            if (col0 >= row_last + 2)
+                full.push_back(t);
+            else
+                diag.push_back(t);
+        }
+    }
+    full.insert(full.end(), diag.begin(), diag.end());
+    return full;
+}
+
+uint32_t pick_graph_steps(uint32_t n) {
+    // aim at a few milliseconds of device work per graph launch
+    const double step_us = (double)pairs_of(n) / 3.0e6 + 6.0;
+    double s = 4000.0 / step_us;
+    if (s < 4) s = 4;
+    if (s > 256) s = 256;
+    return (uint32_t)s;
+}
+
+logo_status rebuild(logo_ctx* c) {
+    if (c->chunk_exec) {
+        cudaGraphExecDestroy(c->chunk_exec);
+        c->chunk_exec = nullptr;
+    }
+    if (c->d_tiles) {
+        cudaFree(c->d_tiles);
+        c->d_tiles = nullptr;
+    }
+    std::vector<uint2> tiles = make_tiles(c->n, c->R, c->NW, c->cb);
+    c->ntiles = (uint32_t)tiles.size();
+    if (c->ntiles) {
+        CK(c, cudaMalloc(&c->d_tiles, sizeof(uint2) * tiles.size()));
+        CK(c, cudaMemcpy(c->d_tiles, tiles.data(), sizeof(uint2) * tiles.size(),
+                         cudaMemcpyHostToDevice));
+    }
+    // the sweep's shared-memory opt-in must be set outside stream capture
+    CK(c, launch_sweep_prepare(sweep_args(c)));
+    c->chunk_steps = pick_graph_steps(c->n);
+    cudaGraph_t g = nullptr;
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const SweepLaunch L = sweep_args(c);
+    const TourBufs T = bufs(c);
+    cudaError_t e = cudaSuccess;
+    for (uint32_t s = 0; s < c->chunk_steps && e == cudaSuccess; ++s) {
+        e = launch_sweep(L, c->stream);
+        if (e == cudaSuccess) e = launch_apply_move(T, c->stream);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(c, LOGO_ERR_CUDA,
+                    std::string("graph capture: ") +
+                        cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&c->chunk_exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(c, e);
+    return LOGO_OK;
+}
+
+logo_status check_route(logo_ctx* c, const uint32_t* route) {
+    if (!route) return fail(c, LOGO_ERR_INVALID_ARG, "route is NULL");
+    std::vector<uint8_t> seen(c->n, 0);
+    for (uint32_t k = 0; k < c->n; ++k) {
+        const uint32_t v = route[k];
+        if (v >= c->n || seen[v])
+            return fail(c, LOGO_ERR_INVALID_ARG,
+                        "route is not a permutation of 0..n-1 (position " +
+                            std::to_string(k) + ")");
+        seen[v] = 1;
+    }
+    return LOGO_OK;
+}
+
+logo_status upload_route(logo_ctx* c, const uint32_t* route) {
+    logo_status s = check_route(c, route);
+    if (s != LOGO_OK) return s;
+    std::memcpy(c->h_route, route, sizeof(uint32_t) * c->n);
+    CK(c, cudaMemcpyAsync(c->d_route[0], c->h_route, sizeof(uint32_t) * c->n,
+                          cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->cur, 0, sizeof(unsigned int), c->stream));
+    CK(c, launch_init_ordered(bufs(c), c->stream));
+    c->have_route = true;
+    return LOGO_OK;
+}
+
+logo_status read_state(logo_ctx* c) {
+    CK(c, cudaMemcpyAsync(c->h_st, c->d_st, sizeof(DevState), cudaMemcpyDeviceToHost,
+                          c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return LOGO_OK;
+}
+
+logo_status status_to_error(logo_ctx* c, unsigned int st) {
+    if (st & kErrTimeout)
+        return fail(c, LOGO_ERR_TIMEOUT, "a device-side wait exceeded its time budget");
+    if (st & kErrBadKey)
+        return fail(c, LOGO_ERR_DEVICE_FAULT, "sweep produced an out-of-range move");
+    if (st & kErrMoveLimit)
+        return fail(c, LOGO_ERR_MOVE_LIMIT, "descent reached max_moves");
+    if (st) return fail(c, LOGO_ERR_DEVICE_FAULT, "device status " + std::to_string(st));
+    return LOGO_OK;
+}
+
+// Descent on the resident tour.  Replays the chunk graph until the device
+// reports convergence (or the move limit).
+logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
+                        uint64_t* sweeps_out, bool reset = true) {
+    if (max_moves == 0) max_moves = ~0ull >> 1;
+    if (reset) CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
+    logo_status s0 = read_state(c);
+    if (s0 != LOGO_OK) return s0;
+    const uint64_t sweeps0 = c->h_st->sweeps;
+    const uint64_t moves0 = reset ? 0 : c->h_st->moves;
+    for (;;) {
+        const uint64_t before = c->h_st->moves;
+        CK(c, cudaGraphLaunch(c->chunk_exec, c->stream));
+        logo_status s = read_state(c);
+        if (s != LOGO_OK) return s;
+        if (c->h_st->converged || c->h_st->status) break;
+        // every replay applies at least one move or converges
+        if (c->h_st->moves == before)
+            return fail(c, LOGO_ERR_DEVICE_FAULT, "descent made no progress");
+    }
+    if (moves_out) *moves_out = c->h_st->moves - moves0;
+    if (sweeps_out) *sweeps_out = c->h_st->sweeps - sweeps0;
+    const unsigned int st = c->h_st->status & ~kErrMoveLimit;
+    if (st) return status_to_error(c, st);
+    if ((c->h_st->status & kErrMoveLimit) && c->h_st->moves >= max_moves &&
+        max_moves != (~0ull >> 1))
+        return LOGO_OK;  // caller asked for a bounded number of moves
+    return LOGO_OK;
+}
+
+logo_status download_route(logo_ctx* c, uint32_t* route, bool best) {
+    const uint32_t* src = best ? c->d_route_best : c->d_route[c->h_st->cur & 1];
+    CK(c, cudaMemcpyAsync(c->h_route, src, sizeof(uint32_t) * c->n,
+                          cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    std::memcpy(route, c->h_route, sizeof(uint32_t) * c->n);
+    return LOGO_OK;
+}
+
+logo_status length_now(logo_ctx* c, uint64_t* len) {
+    CK(c, launch_tour_length(bufs(c), c->stream));
+    logo_status s = read_state(c);
+    if (s != LOGO_OK) return s;
+    *len = c->h_st->length;
+    return LOGO_OK;
+}
+
+void destroy(logo_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->chunk_exec) cudaGraphExecDestroy(c->chunk_exec);
+    cudaFree(c->d_xy);
+    cudaFree(c->d_Q[0]);
+    cudaFree(c->d_Q[1]);
+    cudaFree(c->d_route[0]);
+    cudaFree(c->d_route[1]);
+    cudaFree(c->d_Qbest);
+    cudaFree(c->d_route_best);
+    cudaFree(c->d_st);
+    cudaFree(c->d_tiles);
+    if (c->h_st) cudaFreeHost(c->h_st);
+    if (c->h_route) cudaFreeHost(c->h_route);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+struct Timer {
+    logo_ctx* c;
+    explicit Timer(logo_ctx* cc) : c(cc) { cudaEventRecord(c->ev0, c->stream); }
+    double stop() {
+        cudaEventRecord(c->ev1, c->stream);
+        cudaEventSynchronize(c->ev1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        return ms;
+    }
+};
+
+}  // namespace
+
+namespace logo {
+
+// |exact delta - approximate delta| <= filter_margin(diag) for every pair of
+// an instance whose bounding-box diagonal is diag.  Per distance d <= diag:
+// the nint is within 0.5 + 2^-23 (d + 1) of sqrt(s); the contracted sum of
+// squares is within 2^-23 s of the exact binary32 one; the MUFU square root
+// is within rel_err * d of the true root (rel_err = 2^-20, at least 8x the
+// error measured over all binary32 inputs by tests/test_gpu_sqrt_bound.py).
+// Two distances enter a delta, and the filter's own float arithmetic
+// (three roundings on magnitudes <= 4 diag) adds 3 * 2^-24 * 4 diag.  One
+// unit of slack covers the strict comparison.
+float filter_margin(double diag) {
+    const double rel = std::ldexp(1.0, -20);
+    const double u = std::ldexp(1.0, -24);
+    const double m = 1.0 + 2.0 * diag * (3.0 * u + rel) + 2.0 * std::ldexp(1.0, -23) +
+                     3.0 * u * 4.0 * diag + 1.0;
+    return (float)m;
+}
+
+}  // namespace logo
+
+extern "C" {
+
+const char* logo_version(void) { return kVersion; }
+
+const char* logo_last_error(const logo_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    return g_create_err.c_str();
+}
+
+logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_ctx** out) {
+    if (!out) return fail(nullptr, LOGO_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!coords) return fail(nullptr, LOGO_ERR_INVALID_ARG, "coords is NULL");
+    if (n < 3 || n > LOGO_MAX_CITIES)
+        return fail(nullptr, LOGO_ERR_INVALID_ARG,
+                    "n must be in [3, " + std::to_string(LOGO_MAX_CITIES) + "]");
+    double x0 = coords[0].x, x1 = coords[0].x, y0 = coords[0].y, y1 = coords[0].y;
+    for (uint32_t k = 0; k < n; ++k) {
+        const double x = coords[k].x, y = coords[k].y;
+        if (!std::isfinite(x) || !std::isfinite(y))
+            return fail(nullptr, LOGO_ERR_INVALID_ARG,
+                        "coordinate " + std::to_string(k) + " is not finite");
+        x0 = std::min(x0, x); x1 = std::max(x1, x);
+        y0 = std::min(y0, y); y1 = std::max(y1, y);
+    }
+    const double diag = std::sqrt((x1 - x0) * (x1 - x0) + (y1 - y0) * (y1 - y0));
+    if (!(diag < LOGO_MAX_DIAGONAL))
+        return fail(nullptr, LOGO_ERR_INVALID_ARG,
+                    "coordinate bounding-box diagonal exceeds LOGO_MAX_DIAGONAL");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, LOGO_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= ndev)
+        return fail(nullptr, LOGO_ERR_INVALID_ARG, "device index out of range");
+    if (cudaSetDevice(device) != cudaSuccess)
+        return fail(nullptr, LOGO_ERR_CUDA, "cudaSetDevice failed");
+
+    logo_ctx* c = new logo_ctx();
+    c->device = device;
+    c->n = n;
+    c->diag = diag;
+    c->margin = filter_margin(diag);
+    default_shape(n, c->R, c->NW, c->cb);
+    logo_status s = LOGO_OK;
+    auto bail = [&](logo_status st) {
+        g_create_err = c->err;
+        destroy(c);
+        return st;
+    };
+#define CKC(call)                                                             \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess) {                                              \
+            c->err = std::string(#call) + ": " + cudaGetErrorString(e_);      \
+            return bail(e_ == cudaErrorMemoryAllocation ? LOGO_ERR_OOM         \
+                                                        : LOGO_ERR_CUDA);     \
+        }                                                                     \
+    } while (0)
+    CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CKC(cudaEventCreate(&c->ev0));
+    CKC(cudaEventCreate(&c->ev1));
+    CKC(cudaMalloc(&c->d_xy, sizeof(float2) * n));
+    for (int b = 0; b < 2; ++b) {
+        CKC(cudaMalloc(&c->d_Q[b], sizeof(OrderedCity) * n));
+        CKC(cudaMalloc(&c->d_route[b], sizeof(uint32_t) * n));
+    }
+    CKC(cudaMalloc(&c->d_Qbest, sizeof(OrderedCity) * n));
+    CKC(cudaMalloc(&c->d_route_best, sizeof(uint32_t) * n));
+    CKC(cudaMalloc(&c->d_st, sizeof(DevState)));
+    CKC(cudaMallocHost(&c->h_st, sizeof(DevState)));
+    CKC(cudaMallocHost(&c->h_route, sizeof(uint32_t) * n));
+    std::memset(c->h_st, 0, sizeof(DevState));
+    c->h_st->best_key = kNoMove;
+    c->h_st->converged = 1;
+    CKC(cudaMemcpy(c->d_st, c->h_st, sizeof(DevState), cudaMemcpyHostToDevice));
+    CKC(cudaMemcpy(c->d_xy, coords, sizeof(float2) * n, cudaMemcpyHostToDevice));
+#undef CKC
+    s = rebuild(c);
+    if (s != LOGO_OK) return bail(s);
+    *out = c;
+    return LOGO_OK;
+}
+
+logo_status logo_ctx_destroy(logo_ctx* ctx) {
+    destroy(ctx);
+    return LOGO_OK;
+}
+
+logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
+    if (!c || !info) return LOGO_ERR_INVALID_ARG;
+    info->n = c->n;
+    info->device = c->device;
+    info->rows_per_thread = c->R;
+    info->warps_per_cta = c->NW;
+    info->tile_cols = c->cb;
+    info->tiles = c->ntiles;
+    info->filter_margin = c->margin;
+    info->graph_steps = c->chunk_steps;
+    return LOGO_OK;
+}
+
+logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (!sweep_shape_supported(R, NW) || cb < 16 || cb > 8192)
+        return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape");
+    CK(c, cudaSetDevice(c->device));
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->R = R;
+    c->NW = NW;
+    c->cb = cb;
+    return rebuild(c);
+}
+
+void* logo_ctx_stream(logo_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+logo_status logo_sync(logo_ctx* c) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaStreamSynchronize(c->stream));
+    return LOGO_OK;
+}
+
+logo_status logo_set_route(logo_ctx* c, const uint32_t* route) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaSetDevice(c->device));
+    logo_status s = upload_route(c, route);
+    if (s != LOGO_OK) return s;
+    CK(c, cudaStreamSynchronize(c->stream));
+    return LOGO_OK;
+}
+
+logo_status logo_get_route(logo_ctx* c, uint32_t* route) {
+    if (!c || !route) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    logo_status s = read_state(c);
+    if (s != LOGO_OK) return s;
+    return download_route(c, route, false);
+}
+
+logo_status logo_best_move(logo_ctx* c, const uint32_t* route, logo_move* out) {
+    if (!c || !out) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaSetDevice(c->device));
+    logo_status s = upload_route(c, route);
+    if (s != LOGO_OK) return s;
+    return logo_sweep_resident(c, out);
+}
+
+logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
+    if (!c || !out) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));
+    CK(c, launch_sweep(sweep_args(c), c->stream));
+    logo_status s = read_state(c);
+    if (s != LOGO_OK) return s;
+    if (c->h_st->status) return status_to_error(c, c->h_st->status);
+    const uint64_t k = c->h_st->best_key;
+    if (k == kNoMove) {
+        out->i = 0;
+        out->j = 0;
+        out->minchange = 0;
+    } else {
+        out->i = key_i(k);
+        out->j = key_j(k);
+        out->minchange = key_delta(k);
+    }
+    return LOGO_OK;
+}
+
+logo_status logo_descend_resident(logo_ctx* c, uint64_t max_moves, logo_stats* stats) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    Timer t(c);
+    uint64_t moves = 0, sweeps = 0;
+    logo_status s = run_descent(c, max_moves, &moves, &sweeps);
+    const double ms = t.stop();
+    if (s != LOGO_OK) return s;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->moves = moves;
+        stats->sweeps = sweeps;
+        stats->pair_evals = sweeps * pairs_of(c->n);
+        stats->descents = 1;
+        stats->device_ms = ms;
+    }
+    return LOGO_OK;
+}
+
+logo_status logo_length_resident(logo_ctx* c, uint64_t* len) {
+    if (!c || !len) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    return length_now(c, len);
+}
+
+logo_status logo_tour_length(logo_ctx* c, const uint32_t* route, uint64_t* len) {
+    if (!c || !len) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaSetDevice(c->device));
+    logo_status s = upload_route(c, route);
+    if (s != LOGO_OK) return s;
+    return length_now(c, len);
+}
+
+static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves,
+                                int32_t* trace, uint64_t trace_cap, logo_stats* stats) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaSetDevice(c->device));
+    Timer t(c);
+    logo_status s = upload_route(c, route);
+    if (s != LOGO_OK) return s;
+    uint64_t start_len = 0, final_len = 0, moves = 0, sweeps = 0;
+    if (stats) {
+        s = length_now(c, &start_len);
+        if (s != LOGO_OK) return s;
+    }
+    int* d_log = nullptr;
+    if (trace && trace_cap) {
+        if (trace_cap > 0xFFFFFFFFull / 3) trace_cap = 0xFFFFFFFFull / 3;
+        CK(c, cudaMalloc(&d_log, sizeof(int) * 3 * trace_cap));
+        const unsigned int cap32 = (unsigned int)trace_cap;
+        CK(c, cudaMemcpyAsync(&c->d_st->move_log, &d_log, sizeof(d_log),
+                              cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaMemcpyAsync(&c->d_st->log_cap, &cap32, sizeof(cap32),
+                              cudaMemcpyHostToDevice, c->stream));
+    }
+    s = run_descent(c, max_moves, &moves, &sweeps);
+    if (d_log) {
+        int* null_log = nullptr;
+        const unsigned int zero = 0;
+        cudaMemcpyAsync(&c->d_st->move_log, &null_log, sizeof(null_log),
+                        cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(&c->d_st->log_cap, &zero, sizeof(zero), cudaMemcpyHostToDevice,
+                        c->stream);
+        const uint64_t got = std::min<uint64_t>(moves, trace_cap);
+        cudaError_t e = cudaMemcpyAsync(trace, d_log, sizeof(int) * 3 * got,
+                                        cudaMemcpyDeviceToHost, c->stream);
+        cudaStreamSynchronize(c->stream);
+        cudaFree(d_log);
+        if (s == LOGO_OK && e != cudaSuccess)
+            return fail(c, LOGO_ERR_CUDA, "trace copy failed");
+    }
+    if (s != LOGO_OK) return s;
+    if (stats) {
+        s = length_now(c, &final_len);
+        if (s != LOGO_OK) return s;
+    }
+    s = download_route(c, route, false);
+    const double ms = t.stop();
+    if (s != LOGO_OK) return s;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->moves = moves;
+        stats->sweeps = sweeps;
+        stats->pair_evals = sweeps * pairs_of(c->n);
+        stats->descents = 1;
+        stats->start_length = start_len;
+        stats->final_length = final_len;
+        stats->device_ms = ms;
+    }
+    return LOGO_OK;
+}
+
+logo_status logo_descend(logo_ctx* c, uint32_t* route, uint64_t max_moves,
+                         logo_stats* stats) {
+    return descend_impl(c, route, max_moves, nullptr, 0, stats);
+}
+
+logo_status logo_descend_trace(logo_ctx* c, uint32_t* route, uint64_t max_moves,
+                               int32_t* trace, uint64_t trace_cap, logo_stats* stats) {
+    if (!trace && trace_cap) return fail(c, LOGO_ERR_INVALID_ARG, "trace is NULL");
+    return descend_impl(c, route, max_moves, trace, trace_cap, stats);
+}
+
+logo_status logo_ils(logo_ctx* c, uint32_t* route, uint32_t kicks, uint64_t seed,
+                     int kick_kind, logo_stats* stats) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (kick_kind != LOGO_KICK_SEGMENT && kick_kind != LOGO_KICK_DOUBLE_BRIDGE)
+        return fail(c, LOGO_ERR_INVALID_ARG, "unknown kick kind");
+    CK(c, cudaSetDevice(c->device));
+    Timer t(c);
+    logo_status s = upload_route(c, route);
+    if (s != LOGO_OK) return s;
+    // seed the device PRNG and clear the ILS counters
+    CK(c, cudaMemcpyAsync(&c->d_st->rng, &seed, sizeof(seed), cudaMemcpyHostToDevice,
+                          c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->total_moves, 0, sizeof(unsigned long long), c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->accepted, 0, sizeof(unsigned long long), c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->kicks, 0, sizeof(unsigned long long), c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->sweeps, 0, sizeof(unsigned long long), c->stream));
+    CK(c, launch_tour_length(bufs(c), c->stream));
+    CK(c, launch_save_best(bufs(c), c->stream));
+    s = read_state(c);
+    if (s != LOGO_OK) return s;
+    const uint64_t start_len = c->h_st->best_length;
+    const uint64_t kmax = 64ull * c->n * c->n + 1024;
+    for (uint32_t it = 0;; ++it) {
+        s = run_descent(c, kmax, nullptr, nullptr, it == 0);
+        if (s != LOGO_OK) return s;
+        CK(c, launch_tour_length(bufs(c), c->stream));
+        CK(c, launch_accept(bufs(c), c->stream));
+        if (it == kicks) break;
+        CK(c, launch_kick(bufs(c), kick_kind, c->stream));
+    }
+    s = read_state(c);
+    if (s != LOGO_OK) return s;
+    const DevState fin = *c->h_st;
+    s = download_route(c, route, true);
+    const double ms = t.stop();
+    if (s != LOGO_OK) return s;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->moves = fin.total_moves;
+        stats->sweeps = fin.sweeps;
+        stats->pair_evals = fin.sweeps * pairs_of(c->n);
+        stats->descents = (uint64_t)kicks + 1;
+        stats->kicks = fin.kicks;
+        stats->accepted = fin.accepted;
+        stats->start_length = start_len;
+        stats->final_length = fin.best_length;
+        stats->device_ms = ms;
+    }
+    return LOGO_OK;
+}
+
+}  // extern "C"

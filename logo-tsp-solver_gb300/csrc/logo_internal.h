@@ -1,0 +1,57 @@
+// Host-side declarations shared by the translation units of liblogo_gpu.so.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "logo_device.cuh"
+
+namespace logo {
+
+// ---- single-instance sweep (sweep.cu) ---------------------------------------
+struct SweepLaunch {
+    const OrderedCity* Q0;
+    const OrderedCity* Q1;
+    uint32_t n;
+    const uint2* tiles;  // (row0, col0) per CTA
+    uint32_t ntiles;
+    uint32_t cb;         // columns per tile
+    int R, NW;           // rows per thread, warps per CTA
+    float margin;        // filter margin M
+    DevState* st;
+};
+cudaError_t launch_sweep(const SweepLaunch& L, cudaStream_t s);
+// Sets the kernel attributes of L's shape; call before any stream capture.
+cudaError_t launch_sweep_prepare(const SweepLaunch& L);
+bool sweep_shape_supported(int R, int NW);
+size_t sweep_smem_bytes(uint32_t cb);
+
+// ---- tour maintenance (tour.cu) --------------------------------------------
+struct TourBufs {
+    OrderedCity* Q[2];
+    uint32_t* route[2];
+    OrderedCity* Qbest;
+    uint32_t* route_best;
+    const float2* xy;
+    uint32_t n;
+    DevState* st;
+};
+// Builds Q[0] from xy and route[0] (route already uploaded to route[0]).
+cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s);
+// Prepares *st for a new descent: cur = 0 kept, counters cleared.
+cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,
+                                 cudaStream_t s);
+// Applies the move in st->best_key (or marks convergence).
+cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s);
+// st->length = length of the current tour.
+cudaError_t launch_tour_length(const TourBufs& T, cudaStream_t s);
+// ILS pieces.
+cudaError_t launch_kick(const TourBufs& T, int kind, cudaStream_t s);
+cudaError_t launch_accept(const TourBufs& T, cudaStream_t s);
+cudaError_t launch_save_best(const TourBufs& T, cudaStream_t s);
+
+// Upper bound of |exact delta - approximate delta| for coordinates whose
+// bounding-box diagonal is `diag` (see filter_margin in capi.cu).
+float filter_margin(double diag);
+
+}  // namespace logo

@@ -1,0 +1,264 @@
+// Device-resident tour maintenance: tour-ordered gather, 2-opt move
+// application, tour length, ILS kicks and accept/revert (sm_103a).
+//
+// The tour lives in two buffers (Q[cur], route[cur]); every permutation is a
+// gather from buffer cur into buffer cur^1 followed by a flip of cur made by
+// the last CTA to finish (threadfence + counter, no spinning), so the host
+// never touches the tour between moves.
+//   init_ordered_kernel    ≙ ordered-coordinate gather, CUDASolver.cpp:316-319
+//   apply_move_kernel      ≙ rotate + reverse, twoOptLocalSolver.cpp:41-48
+//   tour_length_kernel     ≙ routeLength, headers.h:170-189
+//   kick_kernel            ≙ ILSGlobalSolver::kick, ILSGlobalSolver.cpp:37-48
+//                            (and the double bridge, which has no reference)
+//   accept_kernel          ≙ accept/revert, ILSGlobalSolverSequential.cpp:87-94
+#include "logo_device.cuh"
+#include "logo_internal.h"
+
+namespace logo {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(uint32_t n) {
+    unsigned g = (n + kThreads - 1) / kThreads;
+    return g < 1 ? 1 : (g > 4096 ? 4096 : g);
+}
+
+// Last-CTA election: true in exactly one thread of the grid, after every
+// CTA has finished its writes.
+__device__ __forceinline__ bool last_block_done(unsigned int* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        *counter = 0;
+        return true;
+    }
+    return false;
+}
+
+__global__ void init_ordered_kernel(const float2* __restrict__ xy,
+                                    const uint32_t* __restrict__ route,
+                                    OrderedCity* __restrict__ Q, uint32_t n) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += gridDim.x * blockDim.x) {
+        const float2 a = xy[route[k]];
+        const float2 b = xy[route[k == 0 ? n - 1 : k - 1]];
+        OrderedCity o;
+        o.x = a.x;
+        o.y = a.y;
+        o.e = (float)exact_dist(b.x, b.y, a.x, a.y);
+        o.pad = 0.f;
+        Q[k] = o;
+    }
+}
+
+__global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves) {
+    st->best_key = kNoMove;
+    st->moves = 0;
+    st->converged = 0;
+    st->done_blocks = 0;
+    st->max_moves = max_moves;
+}
+
+// Gather new[k] = old[src(k)] for a permutation given by its source map,
+// recomputing the incoming edge lengths.
+template <typename Src>
+__device__ __forceinline__ void gather_tour(const OrderedCity* __restrict__ Qs,
+                                            const uint32_t* __restrict__ Rs,
+                                            OrderedCity* __restrict__ Qd,
+                                            uint32_t* __restrict__ Rd, uint32_t n,
+                                            Src src) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += gridDim.x * blockDim.x) {
+        const uint32_t s = src(k);
+        const uint32_t sp = src(k == 0 ? n - 1 : k - 1);
+        const OrderedCity a = Qs[s];
+        const OrderedCity b = Qs[sp];
+        OrderedCity o;
+        o.x = a.x;
+        o.y = a.y;
+        o.e = (float)exact_dist(b.x, b.y, a.x, a.y);
+        o.pad = 0.f;
+        Qd[k] = o;
+        Rd[k] = Rs[s];
+    }
+}
+
+__global__ void apply_move_kernel(TourBufs T) {
+    DevState* st = T.st;
+    if (*(volatile unsigned int*)&st->converged) return;
+    const uint64_t key = *(volatile unsigned long long*)&st->best_key;
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    const uint32_t n = T.n;
+    if (key == kNoMove) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->converged = 1;
+            st->sweeps += 1;
+        }
+        return;
+    }
+    // reported move (i, j+1): p = i < q = j+1 (twoOptLocalSolver.cpp:41-48)
+    const uint32_t p = key_i(key), q = key_j(key);
+    if (!(p >= 1 && q < n && q >= p + 2)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            atomicOr(&st->status, kErrBadKey);
+            st->converged = 1;
+        }
+        return;
+    }
+    gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1], cur ? T.route[0] : T.route[1], n,
+                [=] __device__(uint32_t k) { return rotrev_src(k, p, q, n); });
+    if (last_block_done(&st->done_blocks)) {
+        const unsigned long long m = st->moves;
+        if (st->move_log && m < st->log_cap) {
+            st->move_log[3 * m + 0] = key_delta(key);
+            st->move_log[3 * m + 1] = (int)p;
+            st->move_log[3 * m + 2] = (int)q;
+        }
+        st->moves = m + 1;
+        st->total_moves += 1;
+        st->sweeps += 1;
+        st->best_key = kNoMove;
+        st->cur = cur ^ 1;
+        if (m + 1 >= st->max_moves) {
+            st->converged = 1;
+            atomicOr(&st->status, kErrMoveLimit);
+        }
+    }
+}
+
+__global__ void tour_length_kernel(TourBufs T) {
+    DevState* st = T.st;
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    const OrderedCity* Q = cur ? T.Q[1] : T.Q[0];
+    unsigned long long s = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n;
+         k += gridDim.x * blockDim.x)
+        s += (unsigned long long)Q[k].e;
+    s = warp_sum_u64(s);
+    __shared__ unsigned long long part[kThreads / 32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += part[w];
+        atomicAdd(&st->length_acc, t);
+    }
+    if (last_block_done(&st->len_done)) {
+        st->length = st->length_acc;
+        st->length_acc = 0;
+    }
+}
+
+__global__ void kick_kernel(TourBufs T, int kind) {
+    DevState* st = T.st;
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    uint64_t rng = *(volatile unsigned long long*)&st->rng;
+    const uint32_t n = T.n;
+    if (kind == 1) {
+        uint32_t c[3];
+        for (int k = 0; k < 3; ++k) c[k] = 1 + uniform_below(rng, n - 1);
+        uint32_t t;
+        if (c[1] < c[0]) { t = c[0]; c[0] = c[1]; c[1] = t; }
+        if (c[2] < c[1]) { t = c[1]; c[1] = c[2]; c[2] = t; }
+        if (c[1] < c[0]) { t = c[0]; c[0] = c[1]; c[1] = t; }
+        const uint32_t p1 = c[0], p2 = c[1], p3 = c[2];
+        gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1], cur ? T.route[0] : T.route[1], n,
+                    [=] __device__(uint32_t k) { return bridge_src(k, p1, p2, p3); });
+    } else {
+        uint32_t a = uniform_below(rng, n);
+        uint32_t b = uniform_below(rng, n);
+        if (b < a) { uint32_t t = a; a = b; b = t; }
+        gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1], cur ? T.route[0] : T.route[1], n,
+                    [=] __device__(uint32_t k) { return rotrev_src(k, a, b, n); });
+    }
+    if (last_block_done(&st->done_blocks)) {
+        st->rng = rng;
+        st->cur = cur ^ 1;
+        st->kicks += 1;
+        st->best_key = kNoMove;
+        st->moves = 0;
+        st->converged = 0;
+    }
+}
+
+// After a descent and tour_length_kernel: keep the tour if it is strictly
+// shorter than the best so far, else restore the best.
+__global__ void accept_kernel(TourBufs T) {
+    DevState* st = T.st;
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    const unsigned long long len = *(volatile unsigned long long*)&st->length;
+    const unsigned long long bl = *(volatile unsigned long long*)&st->best_length;
+    const bool take = len < bl;
+    OrderedCity* Qc = cur ? T.Q[1] : T.Q[0];
+    uint32_t* Rc = cur ? T.route[1] : T.route[0];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n;
+         k += gridDim.x * blockDim.x) {
+        if (take) {
+            T.Qbest[k] = Qc[k];
+            T.route_best[k] = Rc[k];
+        } else {
+            Qc[k] = T.Qbest[k];
+            Rc[k] = T.route_best[k];
+        }
+    }
+    if (last_block_done(&st->done_blocks)) {
+        if (take) {
+            st->best_length = len;
+            st->accepted += 1;
+        }
+    }
+}
+
+__global__ void save_best_kernel(TourBufs T) {
+    DevState* st = T.st;
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n;
+         k += gridDim.x * blockDim.x) {
+        T.Qbest[k] = (cur ? T.Q[1] : T.Q[0])[k];
+        T.route_best[k] = (cur ? T.route[1] : T.route[0])[k];
+    }
+    if (last_block_done(&st->done_blocks)) st->best_length = st->length;
+}
+
+}  // namespace
+
+cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s) {
+    init_ordered_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, T.route[0], T.Q[0], T.n);
+    return cudaGetLastError();
+}
+cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,
+                                 cudaStream_t s) {
+    reset_descent_kernel<<<1, 1, 0, s>>>(T.st, max_moves);
+    return cudaGetLastError();
+}
+cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s) {
+    apply_move_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);
+    return cudaGetLastError();
+}
+cudaError_t launch_tour_length(const TourBufs& T, cudaStream_t s) {
+    tour_length_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);
+    return cudaGetLastError();
+}
+cudaError_t launch_kick(const TourBufs& T, int kind, cudaStream_t s) {
+    kick_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T, kind);
+    return cudaGetLastError();
+}
+cudaError_t launch_accept(const TourBufs& T, cudaStream_t s) {
+    accept_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);
+    return cudaGetLastError();
+}
+cudaError_t launch_save_best(const TourBufs& T, cudaStream_t s) {
+    save_best_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);
+    return cudaGetLastError();
+}
+
+}  // namespace logo

@@ -1,0 +1,249 @@
+"""Python binding of the C ABI in include/logo_gpu.h (ctypes, no torch).
+
+The library is liblogo_gpu.so built in this directory by build_lib.py.  There
+is no CPU fallback: if the library cannot be loaded, or no CUDA device is
+present, calls raise.
+
+The class names mirror the reference's solver interface:
+  Solver.optimize_step  ≙ LocalSolver::optimizeStep (src/solvers/localSolver.h:124-125)
+  Solver.optimize       ≙ TwoOptLocalSolver::optimize (src/solvers/twoOptLocalSolver.cpp:22-64)
+  Solver.ils            ≙ ILSGlobalSolverSequential::optimize
+                          (src/solvers/ILSGlobalSolverSequential.cpp:60-100)
+  Solver.route_length   ≙ routeLength (src/headers.h:170-189)
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblogo_gpu.so")
+
+KICK_SEGMENT = 0
+KICK_DOUBLE_BRIDGE = 1
+MAX_CITIES = 2097152
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",
+          6: "MOVE_LIMIT", 7: "NO_DEVICE", 8: "BUSY", 9: "NOT_FOUND"}
+
+# every exported symbol of include/logo_gpu.h (checked by the CPU test suite)
+EXPORTS = [
+    "logo_ctx_create", "logo_ctx_destroy", "logo_last_error", "logo_best_move",
+    "logo_descend", "logo_ils", "logo_tour_length", "logo_set_route", "logo_get_route",
+    "logo_descend_resident", "logo_sweep_resident", "logo_length_resident", "logo_sync",
+    "logo_ctx_get_info", "logo_ctx_set_shape", "logo_ctx_stream", "logo_version",
+    "logo_descend_trace", "logo_diag_sqrt_error",
+]
+
+
+class LogoError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Move(ctypes.Structure):
+    """best2_out (src/defs.h:181-187)."""
+    _fields_ = [("i", ctypes.c_uint32), ("j", ctypes.c_uint32), ("minchange", ctypes.c_int32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("moves", ctypes.c_uint64), ("sweeps", ctypes.c_uint64),
+                ("pair_evals", ctypes.c_uint64), ("descents", ctypes.c_uint64),
+                ("kicks", ctypes.c_uint64), ("accepted", ctypes.c_uint64),
+                ("start_length", ctypes.c_uint64), ("final_length", ctypes.c_uint64),
+                ("device_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CtxInfo(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("device", ctypes.c_int),
+                ("rows_per_thread", ctypes.c_int), ("warps_per_cta", ctypes.c_int),
+                ("tile_cols", ctypes.c_uint32), ("tiles", ctypes.c_uint32),
+                ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32)]
+
+
+_lib = None
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_vp = ctypes.c_void_p
+
+
+def build(force=False):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_logo_build_lib",
+                                                  os.path.join(HERE, "build_lib.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.build(force=force)
+
+
+def load(path=LIB_PATH):
+    """Loads liblogo_gpu.so (raises OSError if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    L = ctypes.CDLL(path)
+    c = ctypes
+    L.logo_version.restype = c.c_char_p
+    L.logo_last_error.restype = c.c_char_p
+    L.logo_last_error.argtypes = [_vp]
+    L.logo_ctx_create.argtypes = [c.c_int, _vp, c.c_uint32, c.POINTER(_vp)]
+    L.logo_ctx_destroy.argtypes = [_vp]
+    L.logo_best_move.argtypes = [_vp, _u32p, c.POINTER(Move)]
+    L.logo_descend.argtypes = [_vp, _u32p, c.c_uint64, c.POINTER(Stats)]
+    L.logo_ils.argtypes = [_vp, _u32p, c.c_uint32, c.c_uint64, c.c_int, c.POINTER(Stats)]
+    L.logo_tour_length.argtypes = [_vp, _u32p, _u64p]
+    L.logo_set_route.argtypes = [_vp, _u32p]
+    L.logo_get_route.argtypes = [_vp, _u32p]
+    L.logo_descend_resident.argtypes = [_vp, c.c_uint64, c.POINTER(Stats)]
+    L.logo_sweep_resident.argtypes = [_vp, c.POINTER(Move)]
+    L.logo_length_resident.argtypes = [_vp, _u64p]
+    L.logo_sync.argtypes = [_vp]
+    L.logo_ctx_get_info.argtypes = [_vp, c.POINTER(CtxInfo)]
+    L.logo_ctx_set_shape.argtypes = [_vp, c.c_int, c.c_int, c.c_uint32]
+    L.logo_ctx_stream.restype = _vp
+    L.logo_ctx_stream.argtypes = [_vp]
+    L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
+                                     c.c_uint64, c.POINTER(Stats)]
+    L.logo_diag_sqrt_error.argtypes = [c.c_int, ctypes.POINTER(ctypes.c_double)]
+    _lib = L
+    return L
+
+
+def _check(status, ctx=None):
+    if status != 0:
+        msg = load().logo_last_error(ctx).decode(errors="replace")
+        raise LogoError(status, msg)
+
+
+def _route_arg(route, n):
+    r = np.ascontiguousarray(route, dtype=np.uint32)
+    if r.shape != (n,):
+        raise ValueError(f"route must have shape ({n},)")
+    return r
+
+
+class Solver:
+    """One instance on one GPU (a logo_ctx)."""
+
+    def __init__(self, coords, device=0):
+        L = load()
+        xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
+        self.n = xy.shape[0]
+        self._xy = xy
+        h = _vp()
+        _check(L.logo_ctx_create(device, xy.ctypes.data, self.n, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().logo_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- reference-shaped API ------------------------------------------------
+    def optimize_step(self, route):
+        """(minchange, i, j) of the best move (best2_out)."""
+        r = _route_arg(route, self.n)
+        m = Move()
+        _check(load().logo_best_move(self._h, r.ctypes.data_as(_u32p), ctypes.byref(m)),
+               self._h)
+        return (m.minchange, m.i, m.j)
+
+    def optimize(self, route, max_moves=0):
+        """2-opt descent; returns (route, stats)."""
+        r = np.array(route, dtype=np.uint32, copy=True)
+        _route_arg(r, self.n)
+        st = Stats()
+        _check(load().logo_descend(self._h, r.ctypes.data_as(_u32p), max_moves,
+                                   ctypes.byref(st)), self._h)
+        return r, st.as_dict()
+
+    def optimize_trace(self, route, max_moves=0, trace_cap=1 << 20):
+        """Descent that also returns the (minchange, i, j) of every move."""
+        r = np.array(route, dtype=np.uint32, copy=True)
+        _route_arg(r, self.n)
+        tr = np.zeros((trace_cap, 3), dtype=np.int32)
+        st = Stats()
+        _check(load().logo_descend_trace(self._h, r.ctypes.data_as(_u32p), max_moves,
+                                         tr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                         trace_cap, ctypes.byref(st)), self._h)
+        return r, tr[: min(st.moves, trace_cap)].copy(), st.as_dict()
+
+    def ils(self, route, kicks, seed, kind=KICK_SEGMENT):
+        r = np.array(route, dtype=np.uint32, copy=True)
+        _route_arg(r, self.n)
+        st = Stats()
+        _check(load().logo_ils(self._h, r.ctypes.data_as(_u32p), kicks, seed, kind,
+                               ctypes.byref(st)), self._h)
+        return r, st.as_dict()
+
+    def route_length(self, route):
+        r = _route_arg(route, self.n)
+        v = ctypes.c_uint64()
+        _check(load().logo_tour_length(self._h, r.ctypes.data_as(_u32p), ctypes.byref(v)),
+               self._h)
+        return v.value
+
+    # -- resident tour ----------------------------------------------------------
+    def set_route(self, route):
+        r = _route_arg(route, self.n)
+        _check(load().logo_set_route(self._h, r.ctypes.data_as(_u32p)), self._h)
+
+    def get_route(self):
+        r = np.zeros(self.n, dtype=np.uint32)
+        _check(load().logo_get_route(self._h, r.ctypes.data_as(_u32p)), self._h)
+        return r
+
+    def descend_resident(self, max_moves=0):
+        st = Stats()
+        _check(load().logo_descend_resident(self._h, max_moves, ctypes.byref(st)), self._h)
+        return st.as_dict()
+
+    def sweep_resident(self):
+        m = Move()
+        _check(load().logo_sweep_resident(self._h, ctypes.byref(m)), self._h)
+        return (m.minchange, m.i, m.j)
+
+    def length_resident(self):
+        v = ctypes.c_uint64()
+        _check(load().logo_length_resident(self._h, ctypes.byref(v)), self._h)
+        return v.value
+
+    def sync(self):
+        _check(load().logo_sync(self._h), self._h)
+
+    def info(self):
+        i = CtxInfo()
+        _check(load().logo_ctx_get_info(self._h, ctypes.byref(i)), self._h)
+        return {k: getattr(i, k) for k, _ in CtxInfo._fields_}
+
+    def set_shape(self, rows_per_thread, warps_per_cta, tile_cols):
+        _check(load().logo_ctx_set_shape(self._h, rows_per_thread, warps_per_cta, tile_cols),
+               self._h)
+
+    @property
+    def stream(self):
+        return load().logo_ctx_stream(self._h)
+
+
+def sqrt_error(device=0):
+    """Largest relative error of the device's approximate sqrt (see
+    logo_diag_sqrt_error)."""
+    v = ctypes.c_double()
+    _check(load().logo_diag_sqrt_error(device, ctypes.byref(v)))
+    return v.value

@@ -1,0 +1,201 @@
+"""Parity of the sm_103a path with the CPU oracle, through the C ABI.
+
+The bar is bit-exactness: every (minchange, i, j), every tour and every length
+must equal the oracle's, which is itself pinned to the reference's own code
+(tests/test_oracle_ref.py, tests/test_oracle_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [5, 6, 7, 8, 9, 13, 31, 50, 64, 65, 100, 257, 500, 1000, 2000, 3001, 5000, 12001]
+
+
+def _instance(inst, n, seed):
+    kind = seed % 3
+    if kind == 0:
+        return inst.uniform_int(n, seed)
+    if kind == 1:
+        return inst.uniform_f32(n, seed, 1.0e4)
+    return inst.clustered(n, seed, side=1.0e6, clusters=max(2, n // 50))
+
+
+def _replay(oracle, route, log, k):
+    r = np.array(route, dtype=np.uint32)
+    for d, i, j in log[:k]:
+        r = oracle.apply_move(r, int(i), int(j))
+    return r
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_best_move_matches_oracle(lg, inst, oracle_mod, n):
+    seeds = range(3) if n > 3000 else range(8)
+    for seed in seeds:
+        xy = _instance(inst, n, seed)
+        r = inst.random_tour(n, seed + 100)
+        with lg.Solver(xy) as s:
+            assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (n, seed)
+
+
+@pytest.mark.parametrize("n", [60, 300, 1000])
+def test_best_move_near_local_optimum(lg, inst, oracle_mod, n):
+    """States late in a descent: small deltas and many ties."""
+    xy = inst.uniform_int(n, 7)
+    r0 = inst.random_tour(n, 7)
+    _, m, log = oracle_mod.descend(xy, r0, log_cap=1 << 20)
+    with lg.Solver(xy) as s:
+        for k in sorted({max(0, m - t) for t in (1, 2, 3, 5, 10, 30)} | {m}):
+            r = _replay(oracle_mod, r0, log, k)
+            assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (n, k)
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 64), (2, 4, 32), (4, 2, 128), (4, 4, 64),
+                                   (4, 8, 256), (8, 4, 1024), (8, 8, 128), (16, 4, 512)])
+def test_every_tile_shape(lg, inst, oracle_mod, shape):
+    for n, seed in ((3001, 1), (777, 2), (70, 3)):
+        xy = _instance(inst, n, seed)
+        r = inst.random_tour(n, seed)
+        with lg.Solver(xy) as s:
+            s.set_shape(*shape)
+            assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (shape, n)
+            got, st = s.optimize(r, max_moves=25)
+            want = r.copy()
+            for _ in range(25):
+                d, i, j = oracle_mod.best_move(xy, want)
+                if d == 0:
+                    break
+                want = oracle_mod.apply_move(want, i, j)
+            assert np.array_equal(got, want), shape
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_descent_move_sequence_plain_workload(lg, inst, oracle_mod, seed):
+    """n=1000 integer coordinates in [0,1e4)^2, random start: the whole move
+    sequence, the final tour and its length equal the oracle's."""
+    xy = inst.uniform_int(1000, seed)
+    r = inst.random_tour(1000, seed)
+    want, m, log = oracle_mod.descend(xy, r, log_cap=1 << 20)
+    with lg.Solver(xy) as s:
+        got, trace, st = s.optimize_trace(r)
+    assert st["moves"] == m
+    assert np.array_equal(trace, log)
+    assert np.array_equal(got, want)
+    assert st["final_length"] == oracle_mod.tour_length(xy, want)
+    assert st["start_length"] == oracle_mod.tour_length(xy, r)
+    assert st["sweeps"] == m + 1
+
+
+@pytest.mark.parametrize("n,kicks,kind", [(200, 40, 0), (200, 40, 1), (523, 25, 0),
+                                          (523, 25, 1), (1500, 6, 1)])
+def test_ils_matches_oracle(lg, inst, oracle_mod, n, kicks, kind):
+    xy = inst.uniform_f32(n, n, 1.0e4)
+    r = inst.random_tour(n, n + 1)
+    want, ost = oracle_mod.ils(xy, r, kicks, 1234 + n, kind)
+    with lg.Solver(xy) as s:
+        got, st = s.ils(r, kicks, 1234 + n, kind)
+    assert np.array_equal(got, want)
+    assert st["final_length"] == ost["best_length"]
+    assert st["start_length"] == ost["start_length"]
+    assert st["moves"] == ost["moves"]
+    assert st["accepted"] == ost["accepted"]
+    assert st["kicks"] == kicks
+
+
+def test_tour_length_and_resident_api(lg, inst, oracle_mod):
+    n = 4000
+    xy = inst.uniform_f32(n, 5, 1.0e6)
+    r = inst.random_tour(n, 5)
+    with lg.Solver(xy) as s:
+        assert s.route_length(r) == oracle_mod.tour_length(xy, r)
+        s.set_route(r)
+        assert np.array_equal(s.get_route(), r)
+        assert s.sweep_resident() == oracle_mod.best_move(xy, r)
+        st = s.descend_resident(max_moves=10)
+        assert st["moves"] == 10
+        want = r.copy()
+        for _ in range(10):
+            d, i, j = oracle_mod.best_move(xy, want)
+            want = oracle_mod.apply_move(want, i, j)
+        assert np.array_equal(s.get_route(), want)
+        assert s.length_resident() == oracle_mod.tour_length(xy, want)
+
+
+def test_degenerate_instances(lg, inst, oracle_mod):
+    rng = np.random.default_rng(3)
+    cases = []
+    # duplicates and ties: integer grid far smaller than n
+    cases.append(np.floor(rng.random((300, 2)) * 12).astype(np.float32))
+    # all points identical (zero-length edges, no improving move)
+    cases.append(np.full((50, 2), 7.0, dtype=np.float32))
+    # collinear points
+    cases.append(np.stack([np.arange(120, dtype=np.float32) * 3,
+                           np.zeros(120, dtype=np.float32)], 1))
+    # tiny and negative coordinates
+    cases.append((rng.random((200, 2)).astype(np.float32) - 0.5) * 1e-3)
+    for xy in cases:
+        n = len(xy)
+        r = inst.random_tour(n, n)
+        want, m, log = oracle_mod.descend(xy, r, log_cap=1 << 20)
+        with lg.Solver(xy) as s:
+            assert s.optimize_step(r) == oracle_mod.best_move(xy, r)
+            got, trace, st = s.optimize_trace(r)
+        assert np.array_equal(trace, log)
+        assert np.array_equal(got, want)
+
+
+def test_small_n_has_no_move(lg, inst):
+    for n in (3, 4):
+        xy = inst.uniform_int(n, 1)
+        with lg.Solver(xy) as s:
+            assert s.optimize_step(np.arange(n)) == (0, 0, 0)
+            got, st = s.optimize(np.arange(n))
+            assert st["moves"] == 0 and np.array_equal(got, np.arange(n))
+
+
+def test_invalid_arguments(lg, inst):
+    xy = inst.uniform_int(100, 1)
+    with lg.Solver(xy) as s:
+        bad = np.arange(100, dtype=np.uint32)
+        bad[5] = 6
+        with pytest.raises(lg.LogoError) as e:
+            s.optimize_step(bad)
+        assert e.value.status == 1
+        bad = np.arange(100, dtype=np.uint32)
+        bad[0] = 100
+        with pytest.raises(lg.LogoError):
+            s.optimize(bad)
+    with pytest.raises(lg.LogoError):
+        lg.Solver(xy[:2])
+    nan = xy.copy()
+    nan[3, 0] = np.nan
+    with pytest.raises(lg.LogoError):
+        lg.Solver(nan)
+    far = xy.copy()
+    far[0] = (3.0e6, 3.0e6)
+    with pytest.raises(lg.LogoError):
+        lg.Solver(far)
+
+
+def test_sqrt_error_bound(lg):
+    """The filter margin assumes the approximate sqrt is within 2^-20
+    relative; require 8x headroom over what the hardware actually does."""
+    err = lg.sqrt_error(0)
+    assert 0 < err <= 2.0 ** -23, err
+
+
+@pytest.mark.parametrize("n,gen", [(100000, "clustered_nn"), (200000, "uniform_random")])
+def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen):
+    """Full-size single sweeps against the oracle's multi-threaded sweep."""
+    if gen == "clustered_nn":
+        xy = inst.clustered(n, 2)
+        r, _ = oracle_mod.nn_tour(xy)
+    else:
+        xy = inst.uniform_f32(n, 3, 1.0e6)
+        r = inst.random_tour(n, 3)
+    threads = os.cpu_count() or 4
+    key = oracle_mod.best_move_key(xy, r, threads=threads)
+    with lg.Solver(xy) as s:
+        assert s.optimize_step(r) == oracle_mod.unpack_key(key)

@@ -151,6 +151,47 @@ logo_status logo_length_resident(logo_ctx *ctx, uint64_t *length);
 /* Waits for the context's stream. */
 logo_status logo_sync(logo_ctx *ctx);
 
+/* ---- stream-ordered primitives (enqueue only; no host synchronisation) ----- */
+
+/* Starts a descent on the resident tour: clears the convergence flag and the
+ * move counter; max_moves = 0 means no limit. */
+logo_status logo_begin_descent(logo_ctx *ctx, uint64_t max_moves);
+/* Enqueues one best-improvement sweep of the resident tour -- the kernel
+ * launch of CUDASolver::executeKernel (src/solvers/CUDASolver.cpp:403-434)
+ * with the argmin reduced on the device.  A no-op once converged. */
+logo_status logo_enqueue_sweep(logo_ctx *ctx);
+/* Enqueues the application of the last sweep's move on the device (the
+ * rotate+reverse of src/solvers/twoOptLocalSolver.cpp:41-48), or sets the
+ * convergence flag when the sweep found no improving move. */
+logo_status logo_enqueue_apply(logo_ctx *ctx);
+/* Waits for the stream and reports moves applied since logo_begin_descent
+ * and whether the descent has converged. */
+logo_status logo_get_progress(logo_ctx *ctx, uint64_t *moves, int *converged);
+
+/* ---- host-side entry points around the path (no GPU needed) -------------------- */
+
+/* Reads a TSPLIB NODE_COORD_SECTION file into coords[0..n) (float x, y, as
+ * readFileCoords does, src/utils/tsp_loader.c:49-162).  Header lines are
+ * parsed by keyword (the reference skips a fixed 3 lines, :72-94).  With
+ * coords = NULL only *n is returned.  NOT_FOUND if the file cannot be
+ * opened, INVALID_ARG if it is malformed or larger than cap. */
+logo_status logo_read_tsplib(const char *path, logo_xy *coords, uint32_t cap, uint32_t *n);
+
+/* Nearest-neighbour start tour from city `start` (initRoute_KD_NN,
+ * src/utils/kdtree_utils.c:279-301, which starts at city 0): repeatedly the
+ * nearest unvisited city by double-precision Euclidean distance, ties to the
+ * lowest id.  Unlike the reference's kd-tree, duplicate points are kept. */
+logo_status logo_nn_tour(const logo_xy *coords, uint32_t n, uint32_t start, uint32_t *route);
+
+/* Seeded random start tour (routeInit with ROUTE_INIT_SHUFFLE,
+ * src/utils/construction.c:129-137, which uses random_shuffle on rand()):
+ * Fisher-Yates driven by SplitMix64. */
+logo_status logo_random_tour(uint32_t n, uint64_t seed, uint32_t *route);
+
+/* 1 if route is a permutation of 0..n-1 with n >= 3 (checkTour,
+ * src/utils/construction.c:152-183, which exit()s instead), else 0. */
+int logo_check_tour(const uint32_t *route, uint32_t n);
+
 /* ---- introspection ------------------------------------------------------------- */
 
 typedef struct logo_ctx_info {

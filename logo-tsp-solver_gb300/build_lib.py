@@ -12,7 +12,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblogo_gpu.so")
-SOURCES = ["sweep.cu", "tour.cu", "capi.cu", "diag.cu"]
+SOURCES = ["sweep.cu", "tour.cu", "capi.cu", "diag.cu", "construct.cpp"]
+# host files whose floating point must not be contracted into FMAs
+NO_CONTRACT = {"construct.cpp"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "-I" + os.path.join(HERE, "..", "include")]
@@ -28,6 +30,8 @@ def nvcc():
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+    if src in NO_CONTRACT:
+        cmd += ["-Xcompiler", "-ffp-contract=off"]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

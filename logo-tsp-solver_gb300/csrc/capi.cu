@@ -453,6 +453,44 @@ logo_status logo_sync(logo_ctx* c) {
     return LOGO_OK;
 }
 
+logo_status logo_begin_descent(logo_ctx* c, uint64_t max_moves) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    if (max_moves == 0) max_moves = ~0ull >> 1;
+    CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
+    return LOGO_OK;
+}
+
+logo_status logo_enqueue_sweep(logo_ctx* c) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    CK(c, launch_sweep(sweep_args(c), c->stream));
+    return LOGO_OK;
+}
+
+logo_status logo_enqueue_apply(logo_ctx* c) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
+    CK(c, cudaSetDevice(c->device));
+    CK(c, launch_apply_move(bufs(c), c->stream));
+    return LOGO_OK;
+}
+
+logo_status logo_get_progress(logo_ctx* c, uint64_t* moves, int* converged) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaSetDevice(c->device));
+    logo_status s = read_state(c);
+    if (s != LOGO_OK) return s;
+    if (moves) *moves = c->h_st->moves;
+    if (converged) *converged = c->h_st->converged ? 1 : 0;
+    const unsigned int st = c->h_st->status & ~kErrMoveLimit;
+    if (st) return status_to_error(c, st);
+    return LOGO_OK;
+}
+
 logo_status logo_set_route(logo_ctx* c, const uint32_t* route) {
     if (!c) return LOGO_ERR_INVALID_ARG;
     CK(c, cudaSetDevice(c->device));

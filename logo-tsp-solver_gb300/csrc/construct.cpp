@@ -1,0 +1,244 @@
+// Host-side solver entry points around the 2-opt path: TSPLIB parse, start
+// tours and the tour check.  No GPU is needed for any function in this file.
+//
+//   logo_read_tsplib   ≙ readFileCoords       src/utils/tsp_loader.c:49-162
+//   logo_nn_tour       ≙ initRoute_KD_NN      src/utils/kdtree_utils.c:279-301
+//   logo_random_tour   ≙ routeInit(SHUFFLE)   src/utils/construction.c:129-137
+//   logo_check_tour    ≙ checkTour            src/utils/construction.c:152-183
+//
+// Compiled with -ffp-contract=off: the nearest-neighbour search compares
+// double distances and must not change with the host's FMA contraction.
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/logo_gpu.h"
+
+namespace {
+
+uint64_t splitmix64(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Uniform bucket grid over the bounding box with live-item lists per cell;
+// nearest-neighbour queries scan square rings of cells outward and stop once
+// a ring's closest possible point is farther than the best found.
+class NNGrid {
+public:
+    NNGrid(const logo_xy* p, uint32_t n) : p_(p), n_(n) {
+        double x0 = p[0].x, x1 = p[0].x, y0 = p[0].y, y1 = p[0].y;
+        for (uint32_t k = 1; k < n; ++k) {
+            x0 = std::min(x0, (double)p[k].x); x1 = std::max(x1, (double)p[k].x);
+            y0 = std::min(y0, (double)p[k].y); y1 = std::max(y1, (double)p[k].y);
+        }
+        x0_ = x0;
+        y0_ = y0;
+        const double w = std::max(x1 - x0, 1e-30), h = std::max(y1 - y0, 1e-30);
+        const double target = std::max(1.0, n / 2.0);
+        double cell = std::sqrt(w * h / target);
+        if (!(cell > 0)) cell = std::max(w, h);
+        gw_ = (uint32_t)std::min<double>(4096.0, std::floor(w / cell) + 1);
+        gh_ = (uint32_t)std::min<double>(4096.0, std::floor(h / cell) + 1);
+        cw_ = w / gw_;
+        ch_ = h / gh_;
+        start_.assign((size_t)gw_ * gh_ + 1, 0);
+        count_.assign((size_t)gw_ * gh_, 0);
+        items_.resize(n);
+        pos_.resize(n);
+        cell_.resize(n);
+        for (uint32_t k = 0; k < n; ++k) {
+            cell_[k] = cell_of(p[k].x, p[k].y);
+            count_[cell_[k]]++;
+        }
+        for (size_t c = 0; c < count_.size(); ++c) start_[c + 1] = start_[c] + count_[c];
+        std::fill(count_.begin(), count_.end(), 0);
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t c = cell_[k];
+            pos_[k] = start_[c] + count_[c]++;
+            items_[pos_[k]] = k;
+        }
+        live_cells_ = 0;
+        for (uint32_t c : count_) live_cells_ += c ? 1 : 0;
+    }
+
+    // Nearest live city to (px, py) by double Euclidean distance; ties go to
+    // the lower id.
+    uint32_t nearest(double px, double py) const {
+        uint32_t cx, cy;
+        cell_xy(px, py, cx, cy);
+        double best = INFINITY;
+        uint32_t besti = UINT32_MAX;
+        const uint32_t maxr = std::max(gw_, gh_);
+        const double step = std::min(cw_, ch_);
+        for (uint32_t r = 0; r <= maxr; ++r) {
+            if (besti != UINT32_MAX && ((double)r - 1.0) * step > best) break;
+            const int64_t xa = (int64_t)cx - r, xb = (int64_t)cx + r;
+            const int64_t ya = (int64_t)cy - r, yb = (int64_t)cy + r;
+            for (int64_t y = std::max<int64_t>(ya, 0); y <= std::min<int64_t>(yb, gh_ - 1); ++y) {
+                if (y == ya || y == yb) {  // full row of the ring
+                    for (int64_t x = std::max<int64_t>(xa, 0);
+                         x <= std::min<int64_t>(xb, gw_ - 1); ++x)
+                        scan_cell((size_t)y * gw_ + (size_t)x, px, py, best, besti);
+                } else {  // only the two side cells
+                    if (xa >= 0) scan_cell((size_t)y * gw_ + (size_t)xa, px, py, best, besti);
+                    if (xb != xa && xb < (int64_t)gw_)
+                        scan_cell((size_t)y * gw_ + (size_t)xb, px, py, best, besti);
+                }
+            }
+        }
+        return besti;
+    }
+
+    void remove(uint32_t id) {
+        const uint32_t c = cell_[id];
+        const uint32_t last = start_[c] + count_[c] - 1;
+        const uint32_t moved = items_[last];
+        items_[pos_[id]] = moved;
+        pos_[moved] = pos_[id];
+        items_[last] = id;
+        pos_[id] = last;
+        count_[c]--;
+    }
+
+private:
+    void scan_cell(size_t c, double px, double py, double& best, uint32_t& besti) const {
+        for (uint32_t t = 0; t < count_[c]; ++t) {
+            const uint32_t id = items_[start_[c] + t];
+            const double dx = px - (double)p_[id].x, dy = py - (double)p_[id].y;
+            const double d = std::sqrt(dx * dx + dy * dy);
+            if (d < best || (d == best && id < besti)) {
+                best = d;
+                besti = id;
+            }
+        }
+    }
+    uint32_t cell_of(double x, double y) const {
+        uint32_t cx, cy;
+        cell_xy(x, y, cx, cy);
+        return cy * gw_ + cx;
+    }
+    void cell_xy(double x, double y, uint32_t& cx, uint32_t& cy) const {
+        double fx = (x - x0_) / cw_, fy = (y - y0_) / ch_;
+        cx = fx <= 0 ? 0 : (uint32_t)std::min<double>(gw_ - 1, std::floor(fx));
+        cy = fy <= 0 ? 0 : (uint32_t)std::min<double>(gh_ - 1, std::floor(fy));
+    }
+    const logo_xy* p_;
+    uint32_t n_;
+    double x0_, y0_, cw_, ch_;
+    uint32_t gw_, gh_;
+    std::vector<uint32_t> start_, count_, items_, pos_, cell_;
+    uint32_t live_cells_;
+};
+
+bool finite_coords(const logo_xy* c, uint32_t n) {
+    for (uint32_t k = 0; k < n; ++k)
+        if (!std::isfinite(c[k].x) || !std::isfinite(c[k].y)) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+logo_status logo_nn_tour(const logo_xy* coords, uint32_t n, uint32_t start, uint32_t* route) {
+    if (!coords || !route || n == 0 || n > LOGO_MAX_CITIES || start >= n)
+        return LOGO_ERR_INVALID_ARG;
+    if (!finite_coords(coords, n)) return LOGO_ERR_INVALID_ARG;
+    NNGrid g(coords, n);
+    // the reference searches from city 0's own point, so the first pick is
+    // city 0 itself (or an earlier-id duplicate of it)
+    double px = coords[start].x, py = coords[start].y;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t id = g.nearest(px, py);
+        if (id == UINT32_MAX) return LOGO_ERR_INVALID_ARG;
+        route[k] = id;
+        g.remove(id);
+        px = coords[id].x;
+        py = coords[id].y;
+    }
+    return LOGO_OK;
+}
+
+logo_status logo_random_tour(uint32_t n, uint64_t seed, uint32_t* route) {
+    if (!route || n == 0 || n > LOGO_MAX_CITIES) return LOGO_ERR_INVALID_ARG;
+    // Fisher-Yates driven by SplitMix64 from the state seed + 6*C, the same
+    // stream the Python generators use for start tours
+    uint64_t s = seed + 6ull * 0xD1B54A32D192ED03ull;
+    for (uint32_t k = 0; k < n; ++k) route[k] = k;
+    for (uint32_t k = n - 1; k >= 1; --k) {
+        const uint64_t hi = splitmix64(s) >> 32;
+        const uint32_t j = (uint32_t)((hi * (uint64_t)(k + 1)) >> 32);
+        std::swap(route[k], route[j]);
+    }
+    return LOGO_OK;
+}
+
+int logo_check_tour(const uint32_t* route, uint32_t n) {
+    if (!route || n < 3) return 0;
+    std::vector<uint8_t> seen(n, 0);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (route[k] >= n || seen[route[k]]) return 0;
+        seen[route[k]] = 1;
+    }
+    return 1;
+}
+
+// TSPLIB reader.  The reference skips exactly three header lines and then
+// expects "DIMENSION: n" (src/utils/tsp_loader.c:72-102), which misreads
+// files with more header lines; this reader parses "KEY : value" lines until
+// NODE_COORD_SECTION, then reads "id x y" triples (coordinates as float, as
+// the reference does, :127-131) until EOF or a non-numeric token.
+logo_status logo_read_tsplib(const char* path, logo_xy* coords, uint32_t cap, uint32_t* n_out) {
+    if (!path || !n_out) return LOGO_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return LOGO_ERR_NOT_FOUND;
+    char line[4096];
+    long dim = -1;
+    bool in_coords = false;
+    while (std::fgets(line, sizeof line, f)) {
+        std::string s(line);
+        const size_t colon = s.find(':');
+        std::string key = s.substr(0, colon == std::string::npos ? s.size() : colon);
+        key.erase(std::remove_if(key.begin(), key.end(), ::isspace), key.end());
+        if (key == "NODE_COORD_SECTION") {
+            in_coords = true;
+            break;
+        }
+        if (key == "DIMENSION" && colon != std::string::npos)
+            dim = std::strtol(s.c_str() + colon + 1, nullptr, 10);
+    }
+    if (!in_coords || dim <= 0 || (uint64_t)dim > LOGO_MAX_CITIES) {
+        std::fclose(f);
+        return LOGO_ERR_INVALID_ARG;
+    }
+    *n_out = (uint32_t)dim;
+    if (!coords) {  // size query
+        std::fclose(f);
+        return LOGO_OK;
+    }
+    if ((uint32_t)dim > cap) {
+        std::fclose(f);
+        return LOGO_ERR_INVALID_ARG;
+    }
+    long got = 0;
+    long id;
+    float x, y;
+    while (got < dim && std::fscanf(f, "%ld %f %f", &id, &x, &y) == 3) {
+        coords[got].x = x;
+        coords[got].y = y;
+        ++got;
+    }
+    std::fclose(f);
+    if (got != dim) return LOGO_ERR_INVALID_ARG;
+    return LOGO_OK;
+}
+
+}  // extern "C"

@@ -32,7 +32,9 @@ EXPORTS = [
     "logo_descend", "logo_ils", "logo_tour_length", "logo_set_route", "logo_get_route",
     "logo_descend_resident", "logo_sweep_resident", "logo_length_resident", "logo_sync",
     "logo_ctx_get_info", "logo_ctx_set_shape", "logo_ctx_stream", "logo_version",
-    "logo_descend_trace", "logo_diag_sqrt_error",
+    "logo_descend_trace", "logo_diag_sqrt_error", "logo_begin_descent",
+    "logo_enqueue_sweep", "logo_enqueue_apply", "logo_get_progress",
+    "logo_read_tsplib", "logo_nn_tour", "logo_random_tour", "logo_check_tour",
 ]
 
 
@@ -109,6 +111,14 @@ def load(path=LIB_PATH):
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
                                      c.c_uint64, c.POINTER(Stats)]
     L.logo_diag_sqrt_error.argtypes = [c.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.logo_begin_descent.argtypes = [_vp, c.c_uint64]
+    L.logo_enqueue_sweep.argtypes = [_vp]
+    L.logo_enqueue_apply.argtypes = [_vp]
+    L.logo_get_progress.argtypes = [_vp, _u64p, ctypes.POINTER(ctypes.c_int)]
+    L.logo_read_tsplib.argtypes = [c.c_char_p, _vp, c.c_uint32, _u32p]
+    L.logo_nn_tour.argtypes = [_vp, c.c_uint32, c.c_uint32, _u32p]
+    L.logo_random_tour.argtypes = [c.c_uint32, c.c_uint64, _u32p]
+    L.logo_check_tour.argtypes = [_u32p, c.c_uint32]
     _lib = L
     return L
 
@@ -164,14 +174,16 @@ class Solver:
                self._h)
         return (m.minchange, m.i, m.j)
 
-    def optimize(self, route, max_moves=0):
-        """2-opt descent; returns (route, stats)."""
-        r = np.array(route, dtype=np.uint32, copy=True)
+    def optimize(self, route, max_moves=0, stats=True, out=None):
+        """2-opt descent; returns (route, stats).  With stats=False no length
+        is computed (stats is None); `out` may supply the result array."""
+        r = out if out is not None else np.empty(self.n, dtype=np.uint32)
+        r[:] = route
         _route_arg(r, self.n)
-        st = Stats()
+        st = Stats() if stats else None
         _check(load().logo_descend(self._h, r.ctypes.data_as(_u32p), max_moves,
-                                   ctypes.byref(st)), self._h)
-        return r, st.as_dict()
+                                   ctypes.byref(st) if stats else None), self._h)
+        return r, (st.as_dict() if stats else None)
 
     def optimize_trace(self, route, max_moves=0, trace_cap=1 << 20):
         """Descent that also returns the (minchange, i, j) of every move."""
@@ -227,6 +239,22 @@ class Solver:
     def sync(self):
         _check(load().logo_sync(self._h), self._h)
 
+    # -- stream-ordered primitives ----------------------------------------------
+    def begin_descent(self, max_moves=0):
+        _check(load().logo_begin_descent(self._h, max_moves), self._h)
+
+    def enqueue_sweep(self):
+        _check(load().logo_enqueue_sweep(self._h), self._h)
+
+    def enqueue_apply(self):
+        _check(load().logo_enqueue_apply(self._h), self._h)
+
+    def progress(self):
+        m = ctypes.c_uint64()
+        cv = ctypes.c_int()
+        _check(load().logo_get_progress(self._h, ctypes.byref(m), ctypes.byref(cv)), self._h)
+        return m.value, bool(cv.value)
+
     def info(self):
         i = CtxInfo()
         _check(load().logo_ctx_get_info(self._h, ctypes.byref(i)), self._h)
@@ -239,6 +267,35 @@ class Solver:
     @property
     def stream(self):
         return load().logo_ctx_stream(self._h)
+
+
+def read_tsplib(path):
+    """TSPLIB coordinates as an (n, 2) float32 array (host only)."""
+    L = load()
+    n = ctypes.c_uint32()
+    _check(L.logo_read_tsplib(os.fsencode(path), None, 0, ctypes.byref(n)))
+    xy = np.zeros((n.value, 2), dtype=np.float32)
+    _check(L.logo_read_tsplib(os.fsencode(path), xy.ctypes.data, n.value, ctypes.byref(n)))
+    return xy
+
+
+def nn_tour(coords, start=0):
+    """Nearest-neighbour start tour (host only)."""
+    xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
+    r = np.zeros(len(xy), dtype=np.uint32)
+    _check(load().logo_nn_tour(xy.ctypes.data, len(xy), start, r.ctypes.data_as(_u32p)))
+    return r
+
+
+def random_tour(n, seed):
+    r = np.zeros(n, dtype=np.uint32)
+    _check(load().logo_random_tour(n, seed, r.ctypes.data_as(_u32p)))
+    return r
+
+
+def check_tour(route):
+    r = np.ascontiguousarray(route, dtype=np.uint32)
+    return bool(load().logo_check_tour(r.ctypes.data_as(_u32p), len(r)))
 
 
 def sqrt_error(device=0):

@@ -103,3 +103,8 @@ def read_tsp(path):
             b = f.read()
     (n,) = struct.unpack_from("<I", b, 0)
     return np.frombuffer(b, dtype=np.float32, count=2 * n, offset=4).reshape(n, 2).copy()
+
+
+def step(xy, route):
+    """One optimizeStep of the nint solver: (minchange, i, j)."""
+    return struct.unpack_from("<iii", _run("step", xy, route), 0)

@@ -202,6 +202,11 @@ int main(int argc, char **argv) {
         if (!g_log.empty()) fwrite(g_log.data(), 4, g_log.size(), out);
         put_route(out, r);
         put_u64(out, routeLength(r, c.data()));
+    } else if (cmd == "step") {  // one nint optimizeStep
+        NintCPUSolver s(c.data(), &args, n);
+        struct process_time t = s.benchmark(r);
+        int32_t v[3] = {t.out.minchange, (int32_t)t.out.i, (int32_t)t.out.j};
+        fwrite(v, 4, 3, out);
     } else if (cmd == "avxstep") {  // CPUSolver::optimizeStep as shipped (AVX)
         AvxProbe s(c.data(), &args, n);
         struct best2_out o = s.step(r);

@@ -1,0 +1,111 @@
+"""The oracle against golden fixtures produced by the reference's own code
+(tests/golden/make_golden.py, via oracle/_ref/ref_harness).  CPU only."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GENS = ["uniform_int", "uniform_f32", "clustered"]
+
+
+def digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_instance(inst, gen, n, seed):
+    if gen == "uniform_int":
+        return inst.uniform_int(n, seed)
+    if gen == "uniform_f32":
+        return inst.uniform_f32(n, seed, 1.0e4)
+    return inst.clustered(n, seed, side=1.0e6, clusters=max(2, n // 50))
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+def test_single_steps(oracle_mod, inst):
+    g = load("steps.npz")
+    assert len(g["spec"]) >= 300
+    for (gi, n, seed, rseed), out, h in zip(g["spec"], g["out"], g["hash"]):
+        xy = make_instance(inst, GENS[gi], int(n), int(seed))
+        r = inst.random_tour(int(n), int(rseed))
+        assert digest(xy, r) == h, "instance generator drifted"
+        assert oracle_mod.best_move(xy, r) == tuple(int(v) for v in out), (n, seed)
+
+
+@pytest.mark.parametrize("k", range(16))
+def test_descent_move_sequences(oracle_mod, inst, k):
+    g = load("descents_n1000.npz")
+    seed, m, length = (int(v) for v in g["meta"][k])
+    xy = inst.uniform_int(1000, seed)
+    r = inst.random_tour(1000, seed)
+    assert digest(xy, r) == g["hash"][k]
+    fr, mo, log = oracle_mod.descend(xy, r, log_cap=1 << 20)
+    want = g["log"][g["offsets"][k]:g["offsets"][k + 1]]
+    assert mo == m
+    assert np.array_equal(log, want)
+    assert oracle_mod.tour_length(xy, fr) == length
+    assert digest(fr) == g["final_hash"][k]
+
+
+def test_kicks(oracle_mod, inst):
+    g = load("kicks_ils.npz")
+    for (n, seed, kseed, count), h, out, st in zip(g["kick_spec"], g["kick_hash"],
+                                                   g["kick_out"], g["kick_state"]):
+        n, seed = int(n), int(seed)
+        xy = inst.uniform_int(n, seed)
+        r = inst.random_tour(n, seed)
+        assert digest(xy, r) == h
+        s = int(kseed)
+        for _ in range(int(count)):
+            r, s = oracle_mod.kick(r, s)
+        assert digest(r) == out
+        assert s == int(st)
+
+
+def test_ils(oracle_mod, inst):
+    g = load("kicks_ils.npz")
+    for (n, seed, kicks, iseed, bl, moves), h, out in zip(g["ils_spec"], g["ils_hash"],
+                                                          g["ils_out"]):
+        n, seed = int(n), int(seed)
+        xy = inst.uniform_f32(n, seed, 1.0e4)
+        r = inst.random_tour(n, seed)
+        assert digest(xy, r) == h
+        br, st = oracle_mod.ils(xy, r, int(kicks), int(iseed))
+        assert st["best_length"] == bl
+        assert st["moves"] == moves
+        assert digest(br) == out
+
+
+def test_nn_tours(oracle_mod, inst):
+    g = load("nn_tours.npz")
+    for (gi, n, seed), h, out in zip(g["spec"], g["hash"], g["out"]):
+        xy = make_instance(inst, GENS[gi], int(n), int(seed))
+        assert digest(xy) == h
+        t, ties = oracle_mod.nn_tour(xy)
+        assert ties == 0
+        assert digest(t) == out
+
+
+@pytest.mark.parametrize("name", ["berlin52", "kroA100", "pr2392"])
+def test_tsplib_fixtures(oracle_mod, name):
+    g = load("tsplib.npz")
+    xy = g[name + "_xy"]
+    nn = g[name + "_nn"]
+    t, ties = oracle_mod.nn_tour(xy)
+    if ties == 0:  # pr2392 has equidistant candidates; see test_host_entry
+        assert np.array_equal(t, nn)
+    assert oracle_mod.best_move(xy, nn) == tuple(int(v) for v in g[name + "_step"])
+    if name + "_log" in g:
+        fr, m, log = oracle_mod.descend(xy, nn, log_cap=1 << 20)
+        assert np.array_equal(log, g[name + "_log"])
+        assert np.array_equal(fr, g[name + "_final"])
+        final_len, start_len = (int(v) for v in g[name + "_len"])
+        assert oracle_mod.tour_length(xy, fr) == final_len
+        assert oracle_mod.tour_length(xy, nn) == start_len

@@ -168,6 +168,81 @@ logo_status logo_enqueue_apply(logo_ctx *ctx);
  * and whether the descent has converged. */
 logo_status logo_get_progress(logo_ctx *ctx, uint64_t *moves, int *converged);
 
+/* ---- batched solving (no reference counterpart) ------------------------------ */
+
+#define LOGO_BATCH_MAX_N 4096u  /* largest instance of a batch (held in smem) */
+
+/* One instance of a batch.  The caller owns both arrays; route is the start
+ * tour on input and the best tour found on output. */
+typedef struct logo_instance {
+    const logo_xy *coords;
+    uint32_t *route;
+    uint32_t n;
+    uint64_t seed; /* kick PRNG seed (SplitMix64 state) */
+} logo_instance;
+
+/* Tile shape of the batched kernel: rows per thread, threads per CTA (one
+ * CTA per instance), columns per warp tile. */
+typedef struct logo_batch_shape {
+    int rows_per_thread;
+    int threads_per_cta;
+    int tile_cols;
+} logo_batch_shape;
+
+typedef struct logo_batch_opts {
+    int device;
+    uint32_t kicks;         /* ILS kicks per instance; 0 = descent only */
+    int kick_kind;          /* LOGO_KICK_* */
+    logo_batch_shape shape; /* all zero = use the tuned (or default) table */
+    uint32_t ctas;          /* persistent CTAs; 0 = SMs x occupancy */
+} logo_batch_opts;
+
+typedef struct logo_result {
+    uint64_t start_length;
+    uint64_t best_length;
+    uint64_t moves;
+    uint64_t sweeps;
+    uint32_t kicks;
+    uint32_t accepted;
+    int32_t status; /* logo_status of this instance */
+    uint32_t pad;
+} logo_result;
+
+typedef struct logo_batch logo_batch;
+
+/* A reusable batch solver on `device` for up to max_count instances with at
+ * most max_cities cities in total. */
+logo_status logo_batch_create(int device, uint32_t max_count, uint64_t max_cities,
+                              logo_batch **out);
+logo_status logo_batch_destroy(logo_batch *b);
+const char *logo_batch_last_error(const logo_batch *b);
+
+/* Solves every instance independently -- descent, then opts->kicks ILS
+ * iterations, each exactly as logo_ils would -- in one persistent launch per
+ * tile shape used: instances are handed out longest first from a device work
+ * queue, one CTA per instance with the whole instance in shared memory.
+ * Every instance needs 3 <= n <= LOGO_BATCH_MAX_N.  device_ms (optional)
+ * receives the device time of the solve. */
+logo_status logo_batch_run(logo_batch *b, const logo_instance *inst, uint32_t count,
+                           const logo_batch_opts *opts, logo_result *results,
+                           double *device_ms);
+
+/* One-shot logo_batch_create + logo_batch_run + logo_batch_destroy. */
+logo_status logo_batch_solve(const logo_instance *inst, uint32_t count,
+                             const logo_batch_opts *opts, logo_result *results,
+                             double *device_ms);
+
+/* Autotuner: times every compiled tile shape on the given sample per size
+ * bucket (n < 128, < 384, < 1024, < 2048, <= 4096) and installs the fastest
+ * as this batch's table; results are also merged into the JSON file at
+ * cache_path (keyed by GPU name and bucket) when it is not NULL.  With
+ * reuse != 0 a matching cache entry is loaded instead of timing. */
+logo_status logo_batch_autotune(logo_batch *b, const logo_instance *sample, uint32_t count,
+                                uint32_t kicks, int kick_kind, const char *cache_path,
+                                int reuse);
+/* The shape used for instances of size n. */
+logo_status logo_batch_shape_for(const logo_batch *b, uint32_t n, logo_batch_shape *out);
+
 /* ---- host-side entry points around the path (no GPU needed) -------------------- */
 
 /* Reads a TSPLIB NODE_COORD_SECTION file into coords[0..n) (float x, y, as

@@ -1,0 +1,56 @@
+// Host/device interface of the batched persistent solver (batch.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace logo {
+
+constexpr uint32_t kBatchMaxN = 4096;  // largest instance a CTA holds in smem
+
+struct BatchInstance {
+    unsigned long long off;   // first city of this instance in coords / routes
+    unsigned long long seed;  // kick PRNG state
+    uint32_t n;
+    float margin;             // filter margin for this instance's coordinates
+};
+
+struct BatchResult {
+    unsigned long long start_length;
+    unsigned long long best_length;
+    unsigned long long moves;
+    unsigned long long sweeps;
+    uint32_t kicks;
+    uint32_t accepted;
+    uint32_t status;          // kErr* bits
+    uint32_t pad;
+};
+
+struct BatchArgs {
+    const float2* coords;     // all instances' coordinates, concatenated
+    uint32_t* routes;         // start tours in, best tours out
+    const BatchInstance* inst;
+    const uint32_t* order;    // queue order (instances by descending n)
+    BatchResult* results;
+    unsigned int* queue;      // next slot of `order` to hand out
+    uint32_t count;
+    uint32_t max_n;           // sizes the dynamic shared memory
+    uint32_t kicks;
+    int kick_kind;
+};
+
+struct BatchShape {
+    int R;   // rows per thread
+    int NT;  // threads per CTA
+    int TC;  // columns per warp tile
+};
+
+size_t batch_smem_bytes(uint32_t max_n);
+// Launches the persistent kernel with `grid` CTAs; with occupancy != null
+// only reports CTAs per SM for this shape and max_n.
+cudaError_t launch_batch(const BatchArgs& A, const BatchShape& sh, int grid, cudaStream_t s,
+                         int* occupancy);
+// Lists the compiled shapes; returns how many there are.
+int batch_shapes(BatchShape* out, int cap);
+
+}  // namespace logo

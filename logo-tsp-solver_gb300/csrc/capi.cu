@@ -522,6 +522,7 @@ logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));
+    CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
     CK(c, launch_sweep(sweep_args(c), c->stream));
     logo_status s = read_state(c);
     if (s != LOGO_OK) return s;

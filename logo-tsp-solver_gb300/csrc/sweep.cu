@@ -26,92 +26,9 @@
 // memory, and one 64-bit atomicMin per CTA.
 #include "logo_device.cuh"
 #include "logo_internal.h"
+#include "sweep_core.cuh"
 
 namespace logo {
-
-template <int R>
-struct RowBlock {
-    float x[R + 1], y[R + 1];  // rows ib-1 .. ib+R-1
-    float T[R];                // filter threshold of pair row ib+r
-    float Dp[R];               // approx d(ib-1+r, c-1)
-};
-
-template <int R>
-__device__ __forceinline__ void refresh_thresholds(RowBlock<R>& rb,
-                                                   const OrderedCity* Q,
-                                                   uint32_t ib, uint32_t n,
-                                                   int B, float margin) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        uint32_t i = ib + r;
-        if (i + 3 <= n) {
-            int ei = (int)__ldg(&Q[i].e);
-            rb.T[r] = (float)(B + ei) + margin;
-        } else {
-            rb.T[r] = -INFINITY;
-        }
-    }
-}
-
-// Exact re-evaluation of the candidates of column c (rarely taken branch;
-// inlined so that the row block stays in registers).
-template <int R>
-__device__ __forceinline__ void column_exact(RowBlock<R>& rb, const float* Dc,
-                                          const OrderedCity& q,
-                                          const OrderedCity& qp, uint32_t c,
-                                          uint32_t ib, uint32_t n,
-                                          const OrderedCity* Q, float margin,
-                                          int& B, uint64_t& best) {
-    const int ec = (int)q.e;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const uint32_t i = ib + r;
-        const float v = Dc[r + 1] + (rb.Dp[r] - q.e);
-        if (c >= i + 2 && v < rb.T[r]) {
-            const int d1 = exact_dist(rb.x[r + 1], rb.y[r + 1], q.x, q.y);
-            const int d2 = exact_dist(rb.x[r], rb.y[r], qp.x, qp.y);
-            const int ei = (int)__ldg(&Q[i].e);
-            const int delta = d1 + d2 - ei - ec;
-            if (delta <= B) {
-                const uint64_t key = pack_key(delta, i, c);
-                best = key < best ? key : best;
-                if (delta < B) {
-                    B = delta;
-                    refresh_thresholds<R>(rb, Q, ib, n, B, margin);
-                }
-            }
-        }
-    }
-}
-
-template <int R, bool MASK>
-__device__ __forceinline__ void column_step(RowBlock<R>& rb,
-                                            const OrderedCity* cols,
-                                            uint32_t col0, uint32_t c,
-                                            uint32_t ib, uint32_t n,
-                                            const OrderedCity* Q, float margin,
-                                            int& B, uint64_t& best) {
-    const OrderedCity q = cols[c - col0 + 1];
-    float Dc[R + 1];
-#pragma unroll
-    for (int k = 0; k <= R; ++k) Dc[k] = approx_dist(rb.x[k], rb.y[k], q.x, q.y);
-    bool hit = false;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const float v = Dc[r + 1] + (rb.Dp[r] - q.e);
-        const bool cand = v < rb.T[r];
-        if (MASK)
-            hit |= cand && (c >= ib + r + 2);
-        else
-            hit |= cand;
-    }
-    if (hit) {
-        const OrderedCity qp = cols[c - col0];
-        column_exact<R>(rb, Dc, q, qp, c, ib, n, Q, margin, B, best);
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r) rb.Dp[r] = Dc[r];
-}
 
 template <int R, int NW>
 __global__ void __launch_bounds__(NW * 32)
@@ -151,29 +68,10 @@ __global__ void __launch_bounds__(NW * 32)
         if (gk != kNoMove) B = min(B, key_delta(gk));
     }
     RowBlock<R> rb;
-#pragma unroll
-    for (int k = 0; k <= R; ++k) {
-        const uint32_t idx = min(ib - 1 + k, n - 1);
-        const float4 p = __ldg(reinterpret_cast<const float4*>(Q + idx));
-        rb.x[k] = p.x;
-        rb.y[k] = p.y;
-    }
+    load_rows<R>(rb, Q, ib, n);
     refresh_thresholds<R>(rb, Q, ib, n, B, margin);
-
-    const bool staged = mbar_wait_bounded(bar, 0, &st->status);
-    const uint32_t c_first = max(col0, ib + 2);
-    if (staged && ib + 3 <= n && c_first < col_end) {
-        const OrderedCity pc = cols[c_first - col0];
-#pragma unroll
-        for (int r = 0; r < R; ++r) rb.Dp[r] = approx_dist(rb.x[r], rb.y[r], pc.x, pc.y);
-        uint32_t c = c_first;
-        const uint32_t peel_end = min(col_end, ib + R + 1);
-        for (; c < peel_end; ++c)
-            column_step<R, true>(rb, cols, col0, c, ib, n, Q, margin, B, best);
-#pragma unroll 2
-        for (; c < col_end; ++c)
-            column_step<R, false>(rb, cols, col0, c, ib, n, Q, margin, B, best);
-    }
+    if (mbar_wait_bounded(bar, 0, &st->status))
+        walk_columns<R>(rb, cols, col0 - 1, col0, col_end, ib, n, Q, margin, B, best);
 
     best = warp_min_u64(best);
     if (lane == 0) wbest[warp] = best;

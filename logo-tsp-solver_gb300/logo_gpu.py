@@ -35,6 +35,8 @@ EXPORTS = [
     "logo_descend_trace", "logo_diag_sqrt_error", "logo_begin_descent",
     "logo_enqueue_sweep", "logo_enqueue_apply", "logo_get_progress",
     "logo_read_tsplib", "logo_nn_tour", "logo_random_tour", "logo_check_tour",
+    "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
+    "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
 ]
 
 
@@ -65,6 +67,28 @@ class CtxInfo(ctypes.Structure):
                 ("rows_per_thread", ctypes.c_int), ("warps_per_cta", ctypes.c_int),
                 ("tile_cols", ctypes.c_uint32), ("tiles", ctypes.c_uint32),
                 ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32)]
+
+
+class Instance(ctypes.Structure):
+    _fields_ = [("coords", ctypes.c_void_p), ("route", ctypes.c_void_p),
+                ("n", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+class BatchShape(ctypes.Structure):
+    _fields_ = [("rows_per_thread", ctypes.c_int), ("threads_per_cta", ctypes.c_int),
+                ("tile_cols", ctypes.c_int)]
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("kicks", ctypes.c_uint32),
+                ("kick_kind", ctypes.c_int), ("shape", BatchShape), ("ctas", ctypes.c_uint32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("start_length", ctypes.c_uint64), ("best_length", ctypes.c_uint64),
+                ("moves", ctypes.c_uint64), ("sweeps", ctypes.c_uint64),
+                ("kicks", ctypes.c_uint32), ("accepted", ctypes.c_uint32),
+                ("status", ctypes.c_int32), ("pad", ctypes.c_uint32)]
 
 
 _lib = None
@@ -119,6 +143,17 @@ def load(path=LIB_PATH):
     L.logo_nn_tour.argtypes = [_vp, c.c_uint32, c.c_uint32, _u32p]
     L.logo_random_tour.argtypes = [c.c_uint32, c.c_uint64, _u32p]
     L.logo_check_tour.argtypes = [_u32p, c.c_uint32]
+    L.logo_batch_create.argtypes = [c.c_int, c.c_uint32, c.c_uint64, c.POINTER(_vp)]
+    L.logo_batch_destroy.argtypes = [_vp]
+    L.logo_batch_last_error.restype = c.c_char_p
+    L.logo_batch_last_error.argtypes = [_vp]
+    L.logo_batch_run.argtypes = [_vp, _vp, c.c_uint32, c.POINTER(BatchOpts), _vp,
+                                 c.POINTER(c.c_double)]
+    L.logo_batch_solve.argtypes = [_vp, c.c_uint32, c.POINTER(BatchOpts), _vp,
+                                   c.POINTER(c.c_double)]
+    L.logo_batch_autotune.argtypes = [_vp, _vp, c.c_uint32, c.c_uint32, c.c_int, c.c_char_p,
+                                      c.c_int]
+    L.logo_batch_shape_for.argtypes = [_vp, c.c_uint32, c.POINTER(BatchShape)]
     _lib = L
     return L
 
@@ -304,3 +339,80 @@ def sqrt_error(device=0):
     v = ctypes.c_double()
     _check(load().logo_diag_sqrt_error(device, ctypes.byref(v)))
     return v.value
+
+
+def _batch_check(status, b):
+    if status != 0:
+        msg = load().logo_batch_last_error(b).decode(errors="replace")
+        raise LogoError(status, msg)
+
+
+class Batch:
+    """Batched persistent solver (logo_batch).  solve() runs descent + ILS on
+    every instance in one persistent launch per tile shape."""
+
+    def __init__(self, max_count, max_cities, device=0):
+        h = _vp()
+        _batch_check(load().logo_batch_create(device, max_count, max_cities, ctypes.byref(h)),
+                     None)
+        self._h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().logo_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def _pack(coords_list, routes, seeds):
+        xs = [np.ascontiguousarray(c, dtype=np.float32).reshape(-1, 2) for c in coords_list]
+        rs = [np.array(r, dtype=np.uint32, copy=True) for r in routes]
+        arr = (Instance * len(xs))()
+        for k, (x, r) in enumerate(zip(xs, rs)):
+            arr[k].coords = x.ctypes.data
+            arr[k].route = r.ctypes.data
+            arr[k].n = len(r)
+            arr[k].seed = int(seeds[k]) & ((1 << 64) - 1)
+        return arr, xs, rs
+
+    def solve(self, coords_list, routes, seeds, kicks=0, kind=KICK_SEGMENT, shape=None, ctas=0):
+        """Returns (routes, results as a list of dicts, device_ms)."""
+        arr, xs, rs = self._pack(coords_list, routes, seeds)
+        o = BatchOpts()
+        o.device = self.device
+        o.kicks = kicks
+        o.kick_kind = kind
+        if shape:
+            o.shape = BatchShape(*shape)
+        o.ctas = ctas
+        res = (Result * len(rs))()
+        ms = ctypes.c_double()
+        _batch_check(load().logo_batch_run(self._h, arr, len(rs), ctypes.byref(o), res,
+                                           ctypes.byref(ms)), self._h)
+        out = [{k: getattr(r, k) for k, _ in Result._fields_ if k != "pad"} for r in res]
+        return rs, out, ms.value
+
+    def autotune(self, coords_list, routes, seeds, kicks=0, kind=KICK_SEGMENT,
+                 cache_path=None, reuse=False):
+        arr, xs, rs = self._pack(coords_list, routes, seeds)
+        _batch_check(load().logo_batch_autotune(
+            self._h, arr, len(rs), kicks, kind,
+            os.fsencode(cache_path) if cache_path else None, 1 if reuse else 0), self._h)
+
+    def shape_for(self, n):
+        s = BatchShape()
+        _batch_check(load().logo_batch_shape_for(self._h, n, ctypes.byref(s)), self._h)
+        return (s.rows_per_thread, s.threads_per_cta, s.tile_cols)
+

@@ -1,0 +1,94 @@
+"""Batched persistent solver: every instance must end exactly where the
+oracle's ILS (and the single-instance GPU path) ends -- same best tour, same
+best length, same move and acceptance counts."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(inst, count, seed, n_lo=5, n_hi=400, extra=()):
+    ns = list(inst.batch_sizes(count, seed, n_lo, n_hi)) + list(extra)
+    coords, routes, seeds = [], [], []
+    for k, n in enumerate(ns):
+        s = inst.instance_seed(seed, k)
+        coords.append(inst.uniform_f32(int(n), s, 1.0e4) if k % 3 else inst.uniform_int(int(n), s))
+        routes.append(inst.random_tour(int(n), s))
+        seeds.append(s)
+    return coords, routes, seeds
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_batch_matches_oracle_ils(lg, inst, oracle_mod, kind):
+    coords, routes, seeds = _workload(inst, 48, 11 + kind, extra=(3, 4, 5, 6))
+    kicks = 12
+    want_routes, want_len, want_moves = oracle_mod.ils_batch(coords, routes, seeds, kicks, kind,
+                                                             threads=os.cpu_count() or 4)
+    with lg.Batch(len(routes), sum(len(r) for r in routes)) as b:
+        got, res, ms = b.solve(coords, routes, seeds, kicks=kicks, kind=kind)
+    for k in range(len(routes)):
+        assert res[k]["status"] == 0
+        assert res[k]["best_length"] == want_len[k], k
+        assert res[k]["moves"] == want_moves[k], k
+        assert np.array_equal(got[k], want_routes[k]), k
+
+
+def test_every_batch_shape_agrees(lg, inst, oracle_mod):
+    coords, routes, seeds = _workload(inst, 24, 5, n_lo=20, n_hi=900)
+    want_routes, want_len, _ = oracle_mod.ils_batch(coords, routes, seeds, 3, 0,
+                                                    threads=os.cpu_count() or 4)
+    shapes = [(2, 128, 64), (2, 256, 64), (4, 128, 64), (4, 256, 64), (4, 256, 128),
+              (4, 512, 128), (8, 256, 128)]
+    with lg.Batch(len(routes), sum(len(r) for r in routes)) as b:
+        for sh in shapes:
+            got, res, _ = b.solve(coords, routes, seeds, kicks=3, shape=sh)
+            assert [r["best_length"] for r in res] == list(want_len), sh
+            assert all(np.array_equal(g, w) for g, w in zip(got, want_routes)), sh
+
+
+def test_batch_large_instances_match_single_instance_path(lg, inst):
+    ns = [4096, 2500, 1999, 1024, 1023, 384, 383, 127]
+    coords = [inst.uniform_f32(n, 100 + n, 1.0e4) for n in ns]
+    routes = [inst.random_tour(n, 200 + n) for n in ns]
+    seeds = [300 + n for n in ns]
+    with lg.Batch(len(ns), sum(ns)) as b:
+        got, res, _ = b.solve(coords, routes, seeds, kicks=2, kind=1)
+    for k, n in enumerate(ns):
+        with lg.Solver(coords[k]) as s:
+            r, st = s.ils(routes[k], 2, seeds[k], 1)
+        assert np.array_equal(got[k], r), n
+        assert res[k]["best_length"] == st["final_length"], n
+        assert res[k]["moves"] == st["moves"], n
+
+
+def test_batch_autotune_keeps_results(lg, inst, tmp_path):
+    coords, routes, seeds = _workload(inst, 40, 9, n_lo=30, n_hi=1500)
+    cache = str(tmp_path / "tune.json")
+    with lg.Batch(len(routes), sum(len(r) for r in routes)) as b:
+        base, res0, _ = b.solve(coords, routes, seeds, kicks=2)
+        b.autotune(coords, routes, seeds, kicks=2, cache_path=cache)
+        tuned, res1, _ = b.solve(coords, routes, seeds, kicks=2)
+        assert [r["best_length"] for r in res0] == [r["best_length"] for r in res1]
+        assert all(np.array_equal(a, c) for a, c in zip(base, tuned))
+        chosen = [b.shape_for(n) for n in (100, 300, 800, 1500)]
+    text = open(cache).read()
+    assert "|" in text and "[" in text
+    with lg.Batch(len(routes), sum(len(r) for r in routes)) as b2:
+        b2.autotune(coords, routes, seeds, kicks=2, cache_path=cache, reuse=True)
+        assert [b2.shape_for(n) for n in (100, 300, 800, 1500)] == chosen
+
+
+def test_batch_rejects_bad_input(lg, inst):
+    with lg.Batch(4, 10000) as b:
+        xy = inst.uniform_int(5000, 1)
+        with pytest.raises(lg.LogoError):
+            b.solve([xy], [np.arange(5000)], [1])
+        xy = inst.uniform_int(50, 1)
+        bad = np.arange(50)
+        bad[3] = 4
+        with pytest.raises(lg.LogoError):
+            b.solve([xy], [bad], [1])
+        with pytest.raises(lg.LogoError):
+            b.solve([xy] * 5, [np.arange(50)] * 5, [1] * 5)

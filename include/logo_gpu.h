@@ -135,6 +135,29 @@ logo_status logo_tour_length(logo_ctx *ctx, const uint32_t *route, uint64_t *len
 logo_status logo_descend_trace(logo_ctx *ctx, uint32_t *route_inout, uint64_t max_moves,
                                int32_t *trace, uint64_t trace_cap, logo_stats *stats);
 
+/* ---- allocation-free sweep ----------------------------------------------------- */
+
+#define LOGO_NOALLOC_MAX_CITIES 65536u
+
+/* No counterpart in the reference.  A best-improvement sweep for callers that
+ * must not allocate device memory: callers that route every device byte
+ * through their own pool allocator, and callers that cannot afford
+ * cudaMalloc/cudaFree because those may synchronise the device.  All pointers
+ * are device pointers owned by the caller: coords (n cities), route (n city
+ * ids), out (one logo_move, written as logo_best_move would) and status_out
+ * (optional; receives LOGO_OK, or LOGO_ERR_INVALID_ARG when route is not a
+ * permutation of 0..n-1 or the coordinates are unusable).  Work is enqueued
+ * on `stream` (a cudaStream_t; NULL = legacy default stream) and the call
+ * returns without waiting.  It allocates nothing: its working memory is a
+ * fixed static device array of LOGO_NOALLOC_MAX_CITIES cities (1 MiB plus an
+ * 8.25 KiB header) that every GPU loading the library holds until exit.
+ * n above that maximum is rejected with LOGO_ERR_INVALID_ARG.  The first call
+ * on each device looks up the array's device address (make it before any
+ * stream capture).  All calls share the array, so calls whose work overlaps
+ * on the GPU race with each other; the caller must order them. */
+logo_status logo_best_move_noalloc(const logo_xy *coords, const uint32_t *route, uint32_t n,
+                                   logo_move *out, int32_t *status_out, void *stream);
+
 /* ---- resident tour (no host copies between calls) --------------------------- */
 
 /* Uploads a start tour that stays on the device. */

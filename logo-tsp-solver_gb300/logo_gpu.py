@@ -37,6 +37,7 @@ EXPORTS = [
     "logo_read_tsplib", "logo_nn_tour", "logo_random_tour", "logo_check_tour",
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
     "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
+    "logo_best_move_noalloc",
 ]
 
 
@@ -154,6 +155,7 @@ def load(path=LIB_PATH):
     L.logo_batch_autotune.argtypes = [_vp, _vp, c.c_uint32, c.c_uint32, c.c_int, c.c_char_p,
                                       c.c_int]
     L.logo_batch_shape_for.argtypes = [_vp, c.c_uint32, c.POINTER(BatchShape)]
+    L.logo_best_move_noalloc.argtypes = [_vp, _vp, c.c_uint32, _vp, _vp, _vp]
     _lib = L
     return L
 
@@ -416,3 +418,9 @@ class Batch:
         _batch_check(load().logo_batch_shape_for(self._h, n, ctypes.byref(s)), self._h)
         return (s.rows_per_thread, s.threads_per_cta, s.tile_cols)
 
+
+def best_move_noalloc(coords_ptr, route_ptr, n, out_ptr, status_ptr=None, stream=None):
+    """logo_best_move_noalloc on caller-owned device pointers (ints); enqueues
+    on `stream` (a cudaStream_t as int, None = legacy default stream)."""
+    _check(load().logo_best_move_noalloc(coords_ptr, route_ptr, n, out_ptr, status_ptr,
+                                         stream))

@@ -301,6 +301,7 @@ typedef struct logo_ctx_info {
     uint32_t tiles;       /* CTAs per sweep */
     float filter_margin;  /* bound on |exact - approximate delta| */
     uint32_t graph_steps; /* sweep+apply steps per graph launch */
+    int variant;          /* LOGO_SWEEP_* */
 } logo_ctx_info;
 
 logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
@@ -309,6 +310,22 @@ logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
  * tile); used by the autotuner.  Invalid shapes return INVALID_ARG. */
 logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per_cta,
                                uint32_t tile_cols);
+
+/* Sweep kernel variants; all return identical moves.
+ * LOGO_SWEEP_SQUARED (default): pairs are screened with squared distances
+ *   against (B + e_i + e_c + 5)^2, no square root on the fast path.
+ * LOGO_SWEEP_MUFU: screened with approximate square roots (MUFU) and an
+ *   error margin.
+ * LOGO_SWEEP_MUFU_PACKED: the same, issued as paired f32x2 arithmetic. */
+#define LOGO_SWEEP_MUFU 0
+#define LOGO_SWEEP_MUFU_PACKED 1
+#define LOGO_SWEEP_SQUARED 2
+/* Selects variant and tile shape together (logo_ctx_set_shape keeps the
+ * variant).  Shapes per variant: SQUARED (R,NW) in {(2,2),(4,2),(4,4),(8,4),
+ * (8,8),(16,4)}; MUFU {(2,2),(2,4),(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)};
+ * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; 16 <= cols <= 4096. */
+logo_status logo_ctx_set_kernel(logo_ctx *ctx, int variant, int rows_per_thread,
+                                int warps_per_cta, uint32_t tile_cols);
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that
  * time or order work against it. */

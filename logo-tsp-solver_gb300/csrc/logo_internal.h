@@ -17,13 +17,14 @@ struct SweepLaunch {
     uint32_t ntiles;
     uint32_t cb;         // columns per tile
     int R, NW;           // rows per thread, warps per CTA
+    int variant;         // 0 MUFU filter, 1 MUFU filter f32x2, 2 square-root-free
     float margin;        // filter margin M
     DevState* st;
 };
 cudaError_t launch_sweep(const SweepLaunch& L, cudaStream_t s);
 // Sets the kernel attributes of L's shape; call before any stream capture.
 cudaError_t launch_sweep_prepare(const SweepLaunch& L);
-bool sweep_shape_supported(int R, int NW);
+bool sweep_shape_supported(int R, int NW, int variant);
 size_t sweep_smem_bytes(uint32_t cb);
 
 // ---- tour maintenance (tour.cu) --------------------------------------------

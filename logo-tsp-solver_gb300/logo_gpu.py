@@ -21,6 +21,9 @@ LIB_PATH = os.path.join(HERE, "liblogo_gpu.so")
 
 KICK_SEGMENT = 0
 KICK_DOUBLE_BRIDGE = 1
+SWEEP_MUFU = 0
+SWEEP_MUFU_PACKED = 1
+SWEEP_SQUARED = 2
 MAX_CITIES = 2097152
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",
@@ -37,7 +40,7 @@ EXPORTS = [
     "logo_read_tsplib", "logo_nn_tour", "logo_random_tour", "logo_check_tour",
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
     "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
-    "logo_best_move_noalloc",
+    "logo_best_move_noalloc", "logo_ctx_set_kernel",
 ]
 
 
@@ -67,7 +70,8 @@ class CtxInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_uint32), ("device", ctypes.c_int),
                 ("rows_per_thread", ctypes.c_int), ("warps_per_cta", ctypes.c_int),
                 ("tile_cols", ctypes.c_uint32), ("tiles", ctypes.c_uint32),
-                ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32)]
+                ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32),
+                ("variant", ctypes.c_int)]
 
 
 class Instance(ctypes.Structure):
@@ -131,6 +135,7 @@ def load(path=LIB_PATH):
     L.logo_sync.argtypes = [_vp]
     L.logo_ctx_get_info.argtypes = [_vp, c.POINTER(CtxInfo)]
     L.logo_ctx_set_shape.argtypes = [_vp, c.c_int, c.c_int, c.c_uint32]
+    L.logo_ctx_set_kernel.argtypes = [_vp, c.c_int, c.c_int, c.c_int, c.c_uint32]
     L.logo_ctx_stream.restype = _vp
     L.logo_ctx_stream.argtypes = [_vp]
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
@@ -296,6 +301,11 @@ class Solver:
         i = CtxInfo()
         _check(load().logo_ctx_get_info(self._h, ctypes.byref(i)), self._h)
         return {k: getattr(i, k) for k, _ in CtxInfo._fields_}
+
+    def set_kernel(self, variant, rows_per_thread, warps_per_cta, tile_cols):
+        """Variant (SWEEP_MUFU, SWEEP_MUFU_PACKED, SWEEP_SQUARED) and shape."""
+        _check(load().logo_ctx_set_kernel(self._h, variant, rows_per_thread, warps_per_cta,
+                                          tile_cols), self._h)
 
     def set_shape(self, rows_per_thread, warps_per_cta, tile_cols):
         _check(load().logo_ctx_set_shape(self._h, rows_per_thread, warps_per_cta, tile_cols),

@@ -52,15 +52,24 @@ def test_best_move_near_local_optimum(lg, inst, oracle_mod, n):
             assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (n, k)
 
 
-@pytest.mark.parametrize("shape", [(2, 2, 64), (2, 4, 32), (4, 2, 128), (4, 4, 64),
-                                   (4, 8, 256), (8, 4, 1024), (8, 8, 128), (16, 4, 512)])
-def test_every_tile_shape(lg, inst, oracle_mod, shape):
+KERNELS = [(2, 2, 2, 64), (2, 4, 2, 128), (2, 4, 4, 64), (2, 8, 4, 1024), (2, 8, 8, 128),
+           (2, 16, 4, 512),
+           (0, 2, 2, 64), (0, 2, 4, 32), (0, 4, 2, 128), (0, 4, 4, 64), (0, 4, 8, 256),
+           (0, 8, 4, 1024), (0, 8, 8, 128), (0, 16, 4, 512),
+           (1, 4, 2, 64), (1, 4, 4, 128), (1, 8, 4, 1024), (1, 8, 8, 256), (1, 16, 2, 512),
+           (1, 16, 4, 1024)]
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_every_tile_shape(lg, inst, oracle_mod, kernel):
+    """Every sweep variant (squared-distance screen, MUFU screen, packed MUFU
+    screen) and every tile shape choose the oracle's move."""
     for n, seed in ((3001, 1), (777, 2), (70, 3)):
         xy = _instance(inst, n, seed)
         r = inst.random_tour(n, seed)
         with lg.Solver(xy) as s:
-            s.set_shape(*shape)
-            assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (shape, n)
+            s.set_kernel(*kernel)
+            assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (kernel, n)
             got, st = s.optimize(r, max_moves=25)
             want = r.copy()
             for _ in range(25):
@@ -68,7 +77,7 @@ def test_every_tile_shape(lg, inst, oracle_mod, shape):
                 if d == 0:
                     break
                 want = oracle_mod.apply_move(want, i, j)
-            assert np.array_equal(got, want), shape
+            assert np.array_equal(got, want), kernel
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3, 4])

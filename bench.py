@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--e2e-steps", type=int, default=40)
     p.add_argument("--cpu-sweeps", type=int, default=2)
+    p.add_argument("--batched", type=int, default=1, help="include the batched comparison")
+    p.add_argument("--batch-count", type=int, default=4096)
+    p.add_argument("--batch-kicks", type=int, default=200)
+    p.add_argument("--batch-seed", type=int, default=3)
+    p.add_argument("--plain-sample", type=int, default=32)
     return p.parse_args()
 
 
@@ -290,6 +295,9 @@ def run_ours(a, world, rank, local, dist):
         "gpu_launches": 2 * a.steps, "wall_s_timed_region": round(t_wall, 3),
     }
 
+    if a.batched and rank == 0:
+        out["batched"] = run_batched(a, local)
+
     # CPU baseline: the oracle's multi-threaded sweep on this host (rank 0)
     if rank == 0 and a.cpu_sweeps > 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -311,6 +319,57 @@ def run_ours(a, world, rank, local, dist):
         }
     s.close()
     return out
+
+
+def run_batched(a, device):
+    """Batched workload: 4096 instances, n log-uniform in [50, 2000], uniform
+    float32 coordinates in [0,1e4)^2, random start tours, descent + 200
+    segment kicks each, solved in one persistent launch per tile shape (one
+    CUDA graph); against looping the plain single-instance path (logo_ils)
+    over a stratified sample of the same instances, with identical final
+    lengths required on that sample."""
+    count, kicks = a.batch_count, a.batch_kicks
+    coords, routes, seeds = instances.batched_workload(count, a.batch_seed)
+    ns = np.array([len(r) for r in routes], dtype=np.int64)
+    pairs = (ns - 2) * (ns - 3) // 2
+    cache = os.path.join(PKG, "autotune_cache.json")
+    with lg.Batch(count, int(ns.sum()), device=device) as b:
+        # autotune on a stratified sample (reuses a cached table for this GPU)
+        order = np.argsort(ns)
+        tsample = order[np.linspace(0, count - 1, min(count, 256)).astype(int)]
+        t0 = time.perf_counter()
+        b.autotune([coords[k] for k in tsample], [routes[k] for k in tsample],
+                   [seeds[k] for k in tsample], kicks=10, cache_path=cache, reuse=True)
+        tune_s = time.perf_counter() - t0
+        shapes = {str(n): b.shape_for(n) for n in (100, 300, 800, 1500)}
+        b.solve(coords[:64], routes[:64], seeds[:64], kicks=2)  # warm-up
+        got, res, ms = b.solve(coords, routes, seeds, kicks=kicks)
+    sweeps = np.array([r["sweeps"] for r in res], dtype=np.int64)
+    batched = count * (kicks + 1) / (ms / 1e3)
+    # plain: the single-instance path, one instance at a time
+    psample = order[np.linspace(0, count - 1, a.plain_sample).astype(int)]
+    identical = True
+    t0 = time.perf_counter()
+    for k in psample:
+        with lg.Solver(coords[k], device=device) as s:
+            r, st = s.ils(routes[k], kicks, seeds[k], lg.KICK_SEGMENT)
+        identical &= (st["final_length"] == res[k]["best_length"]) and bool(
+            np.array_equal(r, got[k]))
+    plain_s = time.perf_counter() - t0
+    plain = len(psample) * (kicks + 1) / plain_s
+    return {
+        "workload": f"{count} instances, n log-uniform in [50,2000], uniform fp32 in "
+                    f"[0,1e4)^2, random start, descent + {kicks} segment kicks each",
+        "metric": "local-opts/s", "value": batched, "device_s": ms / 1e3,
+        "pair_evals_per_s": float((sweeps * pairs).sum() / (ms / 1e3)),
+        "moves": int(sum(r["moves"] for r in res)),
+        "plain": {"value": plain, "unit": "local-opts/s", "sample": int(len(psample)),
+                  "wall_s": plain_s,
+                  "how": "logo_ils per instance (context create + ILS), stratified by n"},
+        "speedup_vs_plain": batched / plain,
+        "identical_lengths_and_tours_on_sample": bool(identical),
+        "autotuned_shapes": shapes, "autotune_s": tune_s,
+    }
 
 
 def run_reference(a, rank):

@@ -266,6 +266,68 @@ logo_status logo_batch_autotune(logo_batch *b, const logo_instance *sample, uint
 /* The shape used for instances of size n. */
 logo_status logo_batch_shape_for(const logo_batch *b, uint32_t n, logo_batch_shape *out);
 
+/* ---- serving: continuous batching of requests (no reference counterpart) ----- */
+
+typedef struct logo_server logo_server;
+
+typedef struct logo_server_opts {
+    int device;
+    uint64_t mem_budget;    /* device bytes for resident requests; 0 = 2 GiB */
+    uint32_t max_slots;     /* requests with n <= LOGO_BATCH_MAX_N in flight; 0 = SMs x occupancy */
+    uint32_t max_large;     /* larger requests in flight; 0 = 2 */
+    uint32_t kicks;         /* ILS kicks per request after its first descent */
+    int kick_kind;          /* LOGO_KICK_* */
+    uint64_t quantum_pairs; /* pair evaluations per request per round; 0 = 2e7 */
+    uint32_t max_pending;   /* submitted but not admitted; 0 = 1,000,000 */
+} logo_server_opts;
+
+typedef struct logo_request_info {
+    uint64_t start_length;
+    uint64_t best_length;
+    uint64_t moves;
+    uint64_t sweeps;
+    uint32_t n;
+    uint32_t kicks;
+    uint32_t accepted;
+    int32_t status;    /* logo_status of this request */
+    double queue_ms;   /* submit -> admitted to the device */
+    double latency_ms; /* submit -> result available */
+} logo_request_info;
+
+typedef struct logo_server_stats {
+    uint64_t submitted, admitted, completed, failed;
+    uint64_t pending, running_small, running_large;
+    uint64_t rounds;
+    double round_device_ms; /* device time of all rounds */
+    uint64_t mem_in_use, mem_budget;
+} logo_server_stats;
+
+/* Starts a server: a scheduler thread that admits submitted requests while
+ * the device-memory budget and slots allow, keeps their tours resident on the
+ * device and advances all admitted small requests together in rounds of
+ * bounded work (continuous batching: a request that arrives while others run
+ * joins the next round).  Requests with n > LOGO_BATCH_MAX_N run concurrently
+ * through the single-instance path.  Every request is solved exactly as
+ * logo_ils would (descent, then `kicks` kicks with accept/revert), so its
+ * result does not depend on what else is in flight. */
+logo_status logo_server_create(const logo_server_opts *opts, logo_server **out);
+/* Queues a request (inputs are copied; route is the start tour).  Thread
+ * safe.  BUSY when max_pending requests are already waiting. */
+logo_status logo_server_submit(logo_server *s, const logo_xy *coords, uint32_t n,
+                               const uint32_t *route, uint64_t seed, uint64_t *id);
+/* BUSY while the request is queued or running; otherwise copies the best
+ * tour to route_out (n entries, may be NULL), fills info and forgets the
+ * request (NOT_FOUND afterwards).  Returns the request's own status. */
+logo_status logo_server_poll(logo_server *s, uint64_t id, uint32_t *route_out,
+                             logo_request_info *info);
+/* logo_server_poll that waits up to timeout_ms for completion. */
+logo_status logo_server_wait(logo_server *s, uint64_t id, uint32_t timeout_ms,
+                             uint32_t *route_out, logo_request_info *info);
+logo_status logo_server_get_stats(logo_server *s, logo_server_stats *out);
+/* Stops the server; running requests are finished, queued ones dropped. */
+logo_status logo_server_destroy(logo_server *s);
+const char *logo_server_last_error(const logo_server *s);
+
 /* ---- host-side entry points around the path (no GPU needed) -------------------- */
 
 /* Reads a TSPLIB NODE_COORD_SECTION file into coords[0..n) (float x, y, as

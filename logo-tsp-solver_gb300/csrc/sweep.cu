@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(NW * 32)
                  const OrderedCity* __restrict__ Q1, uint32_t n,
                  const uint2* __restrict__ tiles, uint32_t cb, float margin,
                  DevState* st) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     uint64_t* wbest = reinterpret_cast<uint64_t*>(smem_raw + 8);  // NW <= 8
     OrderedCity* cols = reinterpret_cast<OrderedCity*>(smem_raw + 80);
@@ -92,7 +92,7 @@ template <int R, int NW>
 __global__ void __launch_bounds__(NW * 32)
     sweep_kernel3(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                   uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, DevState* st) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     uint64_t* wbest = reinterpret_cast<uint64_t*>(smem_raw + 8);  // NW <= 8
     OrderedCity* cols = reinterpret_cast<OrderedCity*>(smem_raw + 80);

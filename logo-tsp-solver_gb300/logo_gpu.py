@@ -41,6 +41,8 @@ EXPORTS = [
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
     "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
     "logo_best_move_noalloc", "logo_ctx_set_kernel",
+    "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
+    "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
 ]
 
 
@@ -94,6 +96,30 @@ class Result(ctypes.Structure):
                 ("moves", ctypes.c_uint64), ("sweeps", ctypes.c_uint64),
                 ("kicks", ctypes.c_uint32), ("accepted", ctypes.c_uint32),
                 ("status", ctypes.c_int32), ("pad", ctypes.c_uint32)]
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("mem_budget", ctypes.c_uint64),
+                ("max_slots", ctypes.c_uint32), ("max_large", ctypes.c_uint32),
+                ("kicks", ctypes.c_uint32), ("kick_kind", ctypes.c_int),
+                ("quantum_pairs", ctypes.c_uint64), ("max_pending", ctypes.c_uint32)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("start_length", ctypes.c_uint64), ("best_length", ctypes.c_uint64),
+                ("moves", ctypes.c_uint64), ("sweeps", ctypes.c_uint64),
+                ("n", ctypes.c_uint32), ("kicks", ctypes.c_uint32),
+                ("accepted", ctypes.c_uint32), ("status", ctypes.c_int32),
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("pending", ctypes.c_uint64), ("running_small", ctypes.c_uint64),
+                ("running_large", ctypes.c_uint64), ("rounds", ctypes.c_uint64),
+                ("round_device_ms", ctypes.c_double), ("mem_in_use", ctypes.c_uint64),
+                ("mem_budget", ctypes.c_uint64)]
 
 
 _lib = None
@@ -161,6 +187,14 @@ def load(path=LIB_PATH):
                                       c.c_int]
     L.logo_batch_shape_for.argtypes = [_vp, c.c_uint32, c.POINTER(BatchShape)]
     L.logo_best_move_noalloc.argtypes = [_vp, _vp, c.c_uint32, _vp, _vp, _vp]
+    L.logo_server_create.argtypes = [c.POINTER(ServerOpts), c.POINTER(_vp)]
+    L.logo_server_submit.argtypes = [_vp, _vp, c.c_uint32, _u32p, c.c_uint64, _u64p]
+    L.logo_server_poll.argtypes = [_vp, c.c_uint64, _u32p, c.POINTER(RequestInfo)]
+    L.logo_server_wait.argtypes = [_vp, c.c_uint64, c.c_uint32, _u32p, c.POINTER(RequestInfo)]
+    L.logo_server_get_stats.argtypes = [_vp, c.POINTER(ServerStats)]
+    L.logo_server_destroy.argtypes = [_vp]
+    L.logo_server_last_error.restype = c.c_char_p
+    L.logo_server_last_error.argtypes = [_vp]
     _lib = L
     return L
 
@@ -434,3 +468,82 @@ def best_move_noalloc(coords_ptr, route_ptr, n, out_ptr, status_ptr=None, stream
     on `stream` (a cudaStream_t as int, None = legacy default stream)."""
     _check(load().logo_best_move_noalloc(coords_ptr, route_ptr, n, out_ptr, status_ptr,
                                          stream))
+
+
+class Server:
+    """Continuous-batching request server (logo_server)."""
+
+    BUSY = 8
+
+    def __init__(self, kicks=0, kind=KICK_SEGMENT, device=0, mem_budget=0, max_slots=0,
+                 max_large=0, quantum_pairs=0, max_pending=0):
+        o = ServerOpts(device, mem_budget, max_slots, max_large, kicks, kind, quantum_pairs,
+                       max_pending)
+        h = _vp()
+        st = load().logo_server_create(ctypes.byref(o), ctypes.byref(h))
+        if st:
+            raise LogoError(st, load().logo_server_last_error(None).decode(errors="replace"))
+        self._h = h
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().logo_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _err(self, st):
+        raise LogoError(st, load().logo_server_last_error(self._h).decode(errors="replace"))
+
+    def submit(self, coords, route, seed):
+        xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
+        r = np.ascontiguousarray(route, dtype=np.uint32)
+        rid = ctypes.c_uint64()
+        st = load().logo_server_submit(self._h, xy.ctypes.data, len(r), r.ctypes.data_as(_u32p),
+                                       int(seed) & ((1 << 64) - 1), ctypes.byref(rid))
+        if st:
+            self._err(st)
+        self._n[rid.value] = len(r)
+        return rid.value
+
+    def _result(self, st, rid, out, info):
+        if st == self.BUSY:
+            return None
+        self._n.pop(rid, None)
+        d = {k: getattr(info, k) for k, _ in RequestInfo._fields_}
+        if st:
+            d["error"] = STATUS.get(st, st)
+            return None, d
+        return out, d
+
+    def poll(self, rid):
+        """None while running, else (route, info)."""
+        out = np.zeros(self._n[rid], dtype=np.uint32)
+        info = RequestInfo()
+        st = load().logo_server_poll(self._h, rid, out.ctypes.data_as(_u32p), ctypes.byref(info))
+        return self._result(st, rid, out, info)
+
+    def wait(self, rid, timeout_ms=600000):
+        out = np.zeros(self._n[rid], dtype=np.uint32)
+        info = RequestInfo()
+        st = load().logo_server_wait(self._h, rid, timeout_ms, out.ctypes.data_as(_u32p),
+                                     ctypes.byref(info))
+        return self._result(st, rid, out, info)
+
+    def stats(self):
+        s = ServerStats()
+        st = load().logo_server_get_stats(self._h, ctypes.byref(s))
+        if st:
+            self._err(st)
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}

@@ -275,7 +275,7 @@ def run_ours(a, world, rank, local, dist):
         "unit": "TFLOP/s",
         "frac": round(achieved_pairs * OPS_PER_PAIR / peak_ops, 4),
         "traffic": profile_traffic(),
-        "kernel": "logo::sweep_kernel3<8,4> (square-root-free screen, 512-column tiles)",
+        "kernel": "logo::sweep_kernel4<8,4> (packed square-root-free screen, 512-column tiles)",
         "ops_per_pair": "6 FP32 + 4 INT (algorithmic convention, 1 distance/pair)",
         "peak_source": f"152 SMs x 128 FP32/INT32 lanes x sm_max_mhz={sm_max:g} "
                        "(MEASURED_PEAKS.json)",

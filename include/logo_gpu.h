@@ -378,14 +378,18 @@ logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per
  *   against (B + e_i + e_c + 5)^2, no square root on the fast path.
  * LOGO_SWEEP_MUFU: screened with approximate square roots (MUFU) and an
  *   error margin.
- * LOGO_SWEEP_MUFU_PACKED: the same, issued as paired f32x2 arithmetic. */
+ * LOGO_SWEEP_MUFU_PACKED: the same, issued as paired f32x2 arithmetic.
+ * LOGO_SWEEP_SQUARED_PACKED: the squared screen with f32x2 distances and a
+ *   per-row threshold over 32-column windows. */
 #define LOGO_SWEEP_MUFU 0
 #define LOGO_SWEEP_MUFU_PACKED 1
 #define LOGO_SWEEP_SQUARED 2
+#define LOGO_SWEEP_SQUARED_PACKED 3
 /* Selects variant and tile shape together (logo_ctx_set_shape keeps the
  * variant).  Shapes per variant: SQUARED (R,NW) in {(2,2),(4,2),(4,4),(8,4),
  * (8,8),(16,4)}; MUFU {(2,2),(2,4),(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)};
- * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; 16 <= cols <= 4096. */
+ * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED
+ * {(4,4),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096. */
 logo_status logo_ctx_set_kernel(logo_ctx *ctx, int variant, int rows_per_thread,
                                 int warps_per_cta, uint32_t tile_cols);
 

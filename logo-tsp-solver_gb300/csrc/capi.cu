@@ -105,14 +105,15 @@ uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) /
 // Default tile shape by size (overridable through logo_ctx_set_shape and
 // logo_ctx_set_variant).
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
-    // measured on GB300: the square-root-free screen wins on large tours
-    // (n = 100k NN tour: 1.38 vs 1.49 ms; n = 1M: 132 vs 140 ms); on smaller
-    // tours that are still far from a local optimum the MUFU screen passes
-    // fewer pairs (n = 10k random tour: 0.088 vs 0.112 ms).
+    // measured on GB300: on large tours the packed, windowed square-root-free
+    // screen is fastest (n = 100k NN tour: 1.08 ms vs 1.38 unpacked vs 1.45
+    // MUFU; n = 1M random tour: 102.6 ms with 1024-column tiles vs 133.7 vs
+    // 141.4); on smaller tours far from a local optimum the MUFU screen passes
+    // fewer pairs (n = 10k random tour: 0.065 ms vs 0.113 ms).
     variant = LOGO_SWEEP_MUFU;
     if (n >= 40000) {
-        variant = LOGO_SWEEP_SQUARED;
-        R = 8; NW = 4; cb = 512;
+        variant = LOGO_SWEEP_SQUARED_PACKED;
+        R = 8; NW = 4; cb = n >= 500000 ? 1024 : 512;
     } else if (n >= 12000) {
         R = 8; NW = 4; cb = 256;
     } else if (n >= 3000) {
@@ -457,7 +458,7 @@ logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
 
 logo_status logo_ctx_set_kernel(logo_ctx* c, int variant, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
-    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_SQUARED)
+    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_SQUARED_PACKED)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown sweep variant");
     if (!sweep_shape_supported(R, NW, variant) || cb < 16 || cb > 4096)
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape for this variant");

@@ -24,6 +24,7 @@ KICK_DOUBLE_BRIDGE = 1
 SWEEP_MUFU = 0
 SWEEP_MUFU_PACKED = 1
 SWEEP_SQUARED = 2
+SWEEP_SQUARED_PACKED = 3
 MAX_CITIES = 2097152
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",

@@ -57,7 +57,8 @@ KERNELS = [(2, 2, 2, 64), (2, 4, 2, 128), (2, 4, 4, 64), (2, 8, 4, 1024), (2, 8,
            (0, 2, 2, 64), (0, 2, 4, 32), (0, 4, 2, 128), (0, 4, 4, 64), (0, 4, 8, 256),
            (0, 8, 4, 1024), (0, 8, 8, 128), (0, 16, 4, 512),
            (1, 4, 2, 64), (1, 4, 4, 128), (1, 8, 4, 1024), (1, 8, 8, 256), (1, 16, 2, 512),
-           (1, 16, 4, 1024)]
+           (1, 16, 4, 1024),
+           (3, 4, 4, 64), (3, 8, 4, 512), (3, 8, 8, 100), (3, 16, 4, 1024)]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)

@@ -162,7 +162,7 @@ def measured_peaks():
 
 def profile_traffic():
     """DRAM bytes per sweep launch at n=100k from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "sweep_kernel_n100k.md")
+    p = os.path.join(ROOT, "profiles", "sweep_kernel4_n100k.md")
     try:
         with open(p) as f:
             for ln in f:

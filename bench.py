@@ -160,9 +160,18 @@ def measured_peaks():
         return {}
 
 
-def profile_traffic():
-    """DRAM bytes per sweep launch at n=100k from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "sweep_kernel4_n100k.md")
+# sweep kernel per LOGO_SWEEP_* variant: (kernel, screen)
+SWEEP_KERNELS = {0: ("sweep_kernel", "MUFU screen"),
+                 1: ("sweep_kernel2", "packed MUFU screen"),
+                 2: ("sweep_kernel3", "square-root-free screen"),
+                 3: ("sweep_kernel4", "packed square-root-free screen"),
+                 4: ("sweep_kernel5", "fused two-stage square-root-free screen")}
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per sweep launch at n=100k from the committed ncu summary
+    of that kernel (None if there is none)."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_n100k.md")
     try:
         with open(p) as f:
             for ln in f:
@@ -263,6 +272,8 @@ def run_ours(a, world, rank, local, dist):
                    "reversal, route D2H"}
 
     # roofline of the sweep kernel (the dominant kernel)
+    info = s.info()
+    kname, screen = SWEEP_KERNELS[info["variant"]]
     peaks = measured_peaks()
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     mean_sweep_s = statistics.mean(sweep_ms) / 1e3
@@ -274,8 +285,9 @@ def run_ours(a, world, rank, local, dist):
         "peak": round(peak_ops / 1e12, 3),
         "unit": "TFLOP/s",
         "frac": round(achieved_pairs * OPS_PER_PAIR / peak_ops, 4),
-        "traffic": profile_traffic(),
-        "kernel": "logo::sweep_kernel4<8,4> (packed square-root-free screen, 512-column tiles)",
+        "traffic": profile_traffic(kname),
+        "kernel": f"logo::{kname}<{info['rows_per_thread']},{info['warps_per_cta']}> "
+                  f"({screen}, {info['tile_cols']}-column tiles)",
         "ops_per_pair": "6 FP32 + 4 INT (algorithmic convention, 1 distance/pair)",
         "peak_source": f"152 SMs x 128 FP32/INT32 lanes x sm_max_mhz={sm_max:g} "
                        "(MEASURED_PEAKS.json)",

@@ -373,23 +373,29 @@ logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
 logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per_cta,
                                uint32_t tile_cols);
 
-/* Sweep kernel variants; all return identical moves.
- * LOGO_SWEEP_SQUARED (default): pairs are screened with squared distances
- *   against (B + e_i + e_c + 5)^2, no square root on the fast path.
- * LOGO_SWEEP_MUFU: screened with approximate square roots (MUFU) and an
- *   error margin.
+/* Sweep kernel variants; all return identical moves (the default depends on
+ * n, see logo_ctx_info.variant).
+ * LOGO_SWEEP_MUFU: pairs are screened with approximate square roots (MUFU)
+ *   and an error margin.
  * LOGO_SWEEP_MUFU_PACKED: the same, issued as paired f32x2 arithmetic.
+ * LOGO_SWEEP_SQUARED: screened with squared distances against
+ *   (B + e_i + e_c + 5)^2, no square root on the fast path.
  * LOGO_SWEEP_SQUARED_PACKED: the squared screen with f32x2 distances and a
- *   per-row threshold over 32-column windows. */
+ *   per-row threshold over 32-column windows.
+ * LOGO_SWEEP_FUSED: two-stage squared screen with the window threshold
+ *   folded into the sum of squares: d(i, c) for every pair (FADD2/FFMA2, two
+ *   rows at a time), d(i-1, c-1) only where that passes; threads share the
+ *   best delta found so far within a sweep. */
 #define LOGO_SWEEP_MUFU 0
 #define LOGO_SWEEP_MUFU_PACKED 1
 #define LOGO_SWEEP_SQUARED 2
 #define LOGO_SWEEP_SQUARED_PACKED 3
+#define LOGO_SWEEP_FUSED 4
 /* Selects variant and tile shape together (logo_ctx_set_shape keeps the
  * variant).  Shapes per variant: SQUARED (R,NW) in {(2,2),(4,2),(4,4),(8,4),
  * (8,8),(16,4)}; MUFU {(2,2),(2,4),(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)};
- * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED
- * {(4,4),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096. */
+ * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED and
+ * FUSED {(4,4),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096. */
 logo_status logo_ctx_set_kernel(logo_ctx *ctx, int variant, int rows_per_thread,
                                 int warps_per_cta, uint32_t tile_cols);
 

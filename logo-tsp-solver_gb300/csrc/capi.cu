@@ -103,19 +103,27 @@ SweepLaunch sweep_args(const logo_ctx* c) {
 uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) / 2; }
 
 // Default tile shape by size (overridable through logo_ctx_set_shape and
-// logo_ctx_set_variant).
+// logo_ctx_set_kernel).
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
-    // measured on GB300: on large tours the packed, windowed square-root-free
-    // screen is fastest (n = 100k NN tour: 1.08 ms vs 1.38 unpacked vs 1.45
-    // MUFU; n = 1M random tour: 102.6 ms with 1024-column tiles vs 133.7 vs
-    // 141.4); on smaller tours far from a local optimum the MUFU screen passes
-    // fewer pairs (n = 10k random tour: 0.065 ms vs 0.113 ms).
+    // measured on GB300 (one sweep): from n = 15k up the fused two-stage
+    // screen is fastest (n = 100k NN tour: 0.90 ms vs 1.16 ms for the packed
+    // squared screen and 1.72 ms MUFU; n = 20k NN tour: 0.069 ms vs 0.084 MUFU;
+    // n = 1M random tour: 80.6 ms with 8-row blocks and 1024-column tiles vs
+    // 105.6 and 170.2); below that the MUFU screen, whose test is tighter on
+    // short tours, wins (n = 10k NN tour: 0.042 ms vs 0.059 ms).
     variant = LOGO_SWEEP_MUFU;
-    if (n >= 40000) {
-        variant = LOGO_SWEEP_SQUARED_PACKED;
-        R = 8; NW = 4; cb = n >= 500000 ? 1024 : 512;
-    } else if (n >= 12000) {
-        R = 8; NW = 4; cb = 256;
+    if (n >= 500000) {
+        variant = LOGO_SWEEP_FUSED;
+        R = 8; NW = 4; cb = 1024;
+    } else if (n >= 60000) {
+        variant = LOGO_SWEEP_FUSED;
+        R = 4; NW = 4; cb = 512;
+    } else if (n >= 30000) {
+        variant = LOGO_SWEEP_FUSED;
+        R = 4; NW = 4; cb = 256;
+    } else if (n >= 15000) {
+        variant = LOGO_SWEEP_FUSED;
+        R = 4; NW = 4; cb = 128;
     } else if (n >= 3000) {
         R = 4; NW = 4; cb = 128;
     } else {
@@ -458,7 +466,7 @@ logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
 
 logo_status logo_ctx_set_kernel(logo_ctx* c, int variant, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
-    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_SQUARED_PACKED)
+    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_FUSED)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown sweep variant");
     if (!sweep_shape_supported(R, NW, variant) || cb < 16 || cb > 4096)
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape for this variant");

@@ -58,13 +58,15 @@ KERNELS = [(2, 2, 2, 64), (2, 4, 2, 128), (2, 4, 4, 64), (2, 8, 4, 1024), (2, 8,
            (0, 8, 4, 1024), (0, 8, 8, 128), (0, 16, 4, 512),
            (1, 4, 2, 64), (1, 4, 4, 128), (1, 8, 4, 1024), (1, 8, 8, 256), (1, 16, 2, 512),
            (1, 16, 4, 1024),
-           (3, 4, 4, 64), (3, 8, 4, 512), (3, 8, 8, 100), (3, 16, 4, 1024)]
+           (3, 4, 4, 64), (3, 8, 4, 512), (3, 8, 8, 100), (3, 16, 4, 1024),
+           (4, 4, 2, 64), (4, 4, 4, 64), (4, 4, 8, 256), (4, 8, 2, 128), (4, 8, 4, 512),
+           (4, 8, 8, 100), (4, 16, 4, 1024)]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
 def test_every_tile_shape(lg, inst, oracle_mod, kernel):
-    """Every sweep variant (squared-distance screen, MUFU screen, packed MUFU
-    screen) and every tile shape choose the oracle's move."""
+    """Every sweep variant (MUFU, packed MUFU, squared, packed squared and
+    fused screens) and every tile shape choose the oracle's move."""
     for n, seed in ((3001, 1), (777, 2), (70, 3)):
         xy = _instance(inst, n, seed)
         r = inst.random_tour(n, seed)
@@ -79,6 +81,27 @@ def test_every_tile_shape(lg, inst, oracle_mod, kernel):
                     break
                 want = oracle_mod.apply_move(want, i, j)
             assert np.array_equal(got, want), kernel
+
+
+VARIANTS = [(v, 8, 4, 128) for v in range(5)]
+
+
+@pytest.mark.parametrize("kernel", VARIANTS)
+def test_every_variant_near_local_optimum(lg, inst, oracle_mod, kernel):
+    """Late-descent states of n = 3000 and 5000 tours (small deltas, tight
+    screens): every variant chooses the oracle's move.  The states come from
+    a device descent; only the single steps are compared."""
+    for n, seed in ((3000, 11), (5000, 12)):
+        xy = inst.clustered(n, seed, side=1.0e6, clusters=max(2, n // 500))
+        r0 = inst.random_tour(n, seed)
+        with lg.Solver(xy) as s:
+            _, st = s.optimize(r0)
+            m = st["moves"]
+            states = [s.optimize(r0, max_moves=max(0, m - t))[0] for t in (0, 1, 3, 10, 100)]
+        with lg.Solver(xy) as s:
+            s.set_kernel(*kernel)
+            for k, r in enumerate(states):
+                assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (kernel, n, k)
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3, 4])
@@ -196,9 +219,39 @@ def test_sqrt_error_bound(lg):
     assert 0 < err <= 2.0 ** -23, err
 
 
-@pytest.mark.parametrize("n,gen", [(100000, "clustered_nn"), (200000, "uniform_random")])
-def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen):
-    """Full-size single sweeps against the oracle's multi-threaded sweep."""
+FUSED_SHAPES = [(4, 4, 256), (4, 2, 256), (4, 8, 128), (8, 4, 512), (8, 8, 256), (16, 4, 1024)]
+
+
+def test_fused_grouped_path_late_descent(lg, inst, oracle_mod):
+    """n = 40,000 (the fused screen's grouped column walk): the NN start tour
+    and states late in its descent (small deltas, tight screens) choose the
+    oracle's move with every fused tile shape."""
+    n = 40000
+    xy = inst.clustered(n, 21, side=1.0e6, clusters=80, sigma_frac=0.01)
+    r0, _ = oracle_mod.nn_tour(xy)
+    threads = os.cpu_count() or 4
+    with lg.Solver(xy) as s:
+        _, st = s.optimize(r0)
+        m = st["moves"]
+        states = [r0] + [s.optimize(r0, max_moves=m - t)[0] for t in (0, 1, 4)]
+    want = [oracle_mod.unpack_key(oracle_mod.best_move_key(xy, r, threads=threads))
+            for r in states]
+    assert want[1][0] == 0 and want[2][0] < 0
+    with lg.Solver(xy) as s:
+        for R, NW, cb in FUSED_SHAPES:
+            s.set_kernel(lg.SWEEP_FUSED, R, NW, cb)
+            for k, r in enumerate(states):
+                assert s.optimize_step(r) == want[k], ((R, NW, cb), k)
+
+
+@pytest.mark.parametrize("n,gen,variant", [(100000, "clustered_nn", None),
+                                           (100000, "clustered_nn", 2),
+                                           (100000, "clustered_nn", 4),
+                                           (200000, "uniform_random", None),
+                                           (200000, "uniform_random", 4)])
+def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen, variant):
+    """Full-size single sweeps against the oracle's multi-threaded sweep
+    (default kernel and the square-root-free screens)."""
     if gen == "clustered_nn":
         xy = inst.clustered(n, 2)
         r, _ = oracle_mod.nn_tour(xy)
@@ -208,4 +261,6 @@ def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen):
     threads = os.cpu_count() or 4
     key = oracle_mod.best_move_key(xy, r, threads=threads)
     with lg.Solver(xy) as s:
+        if variant is not None:
+            s.set_kernel(variant, 8, 4, 512)
         assert s.optimize_step(r) == oracle_mod.unpack_key(key)

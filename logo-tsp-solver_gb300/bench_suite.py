@@ -157,40 +157,87 @@ def _pct(v, q):
     return float(np.percentile(v, q)) if len(v) else None
 
 
-def _serve_run(pool, rate, duration, kicks, drain, seed):
+def _serve_run(pool, rate, duration, kicks, drain, seed, max_large=0):
+    """Poisson arrivals through logo_server.  A collector thread polls every
+    outstanding request, so a long request does not hide later completions;
+    latencies are the server's own (submit to result)."""
     rng = np.random.default_rng(seed)
     t_arr = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.2) + 10))
     t_arr = t_arr[t_arr < duration]
     picks = rng.integers(0, len(pool), size=len(t_arr))
-    lat, qms, done_at = [], [], []
-    with lg.Server(kicks=kicks, kind=lg.KICK_SEGMENT) as srv:
-        ids = []
+    done = {}
+    outstanding = set()
+    lock = threading.Lock()
+    stop = threading.Event()
+    with lg.Server(kicks=kicks, kind=lg.KICK_SEGMENT, max_large=max_large) as srv:
         t0 = time.perf_counter()
+
+        def collect():
+            while True:
+                last = stop.is_set()
+                with lock:
+                    cur = list(outstanding)
+                for rid in cur:
+                    res = srv.poll(rid)
+                    if res is not None:
+                        done[rid] = (res[1], time.perf_counter() - t0)
+                        with lock:
+                            outstanding.discard(rid)
+                if last:
+                    return
+                time.sleep(0.01)
+
+        th = threading.Thread(target=collect, daemon=True)
+        th.start()
+        n_sub = 0
         for t, p in zip(t_arr, picks):
             now = time.perf_counter() - t0
             if t > now:
                 time.sleep(t - now)
             xy, r, s = pool[p]
-            ids.append(srv.submit(xy, r, s))
+            rid = srv.submit(xy, r, s)
+            with lock:
+                outstanding.add(rid)
+            n_sub += 1
         sub_end = time.perf_counter() - t0
-        deadline = t0 + duration + drain
-        for rid in ids:
-            left = deadline - time.perf_counter()
-            if left <= 0:
-                break
-            res = srv.wait(rid, int(left * 1e3))
-            if res is None:
-                break
-            _, info = res
-            lat.append(info["latency_ms"])
-            qms.append(info["queue_ms"])
+        while time.perf_counter() - t0 < duration + drain:
+            with lock:
+                if not outstanding:
+                    break
+            time.sleep(0.05)
+        stop.set()
+        th.join()
         st = srv.stats()
         wall = time.perf_counter() - t0
-    return {"offered_per_s": rate, "duration_s": duration, "submitted": len(ids),
-            "completed": len(lat), "completed_per_s": len(lat) / wall, "wall_s": wall,
+    infos = [d for d, _ in done.values() if "error" not in d]
+    lat = [d["latency_ms"] for d in infos]
+    work = sum(d["sweeps"] * pairs(d["n"]) for d in infos)
+    return {"offered_per_s": rate, "duration_s": duration, "submitted": n_sub,
+            "completed": len(infos), "completed_per_s": len(infos) / wall, "wall_s": wall,
             "submit_s": sub_end, "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
-            "queue_p50_ms": _pct(qms, 50), "pending_at_end": st["pending"],
-            "rounds": st["rounds"], "round_device_s": st["round_device_ms"] / 1e3}
+            "queue_p50_ms": _pct([d["queue_ms"] for d in infos], 50),
+            "pair_evals_per_s": work / wall, "failed": len(done) - len(infos),
+            "pending_at_end": st["pending"], "rounds": st["rounds"],
+            "round_device_s": st["round_device_ms"] / 1e3}
+
+
+def _characterize(pool, kicks):
+    """Each pool instance once through logo_ils: the work a request needs
+    (pair evaluations) and its one-at-a-time device time."""
+    rows = []
+    for xy, r, s in pool:
+        with lg.Solver(xy) as sol:
+            _, st = sol.ils(r, kicks, s, lg.KICK_SEGMENT)
+        rows.append((len(r), st["pair_evals"], st["device_ms"]))
+    n = np.array([x[0] for x in rows])
+    w = np.array([x[1] for x in rows], dtype=np.float64)
+    ms = np.array([x[2] for x in rows])
+    big = n > 4096
+    return {"instances": len(rows), "mean_pair_evals": float(w.mean()),
+            "work_share_above_4096": float(w[big].sum() / w.sum()),
+            "share_above_4096": float(big.mean()),
+            "mean_device_ms_one_at_a_time": float(ms.mean()),
+            "req_per_s_bound_at_7e12": 7.0e12 / float(w.mean())}
 
 
 def _plain_run(pool, rate, duration, kicks, drain, seed):
@@ -222,10 +269,13 @@ def cmd_serve(a):
     pool = _pool(a.pool, a.seed, a.n_lo, a.n_hi)
     rates = [float(x) for x in a.rates.split(",")]
     res = []
+    if a.characterize:
+        res.append({"characterize": _characterize(pool, a.kicks)})
     for rate in rates:
-        srv = _serve_run(pool, rate, a.duration, a.kicks, a.drain, a.seed)
-        plain = _plain_run(pool, rate, a.duration, a.kicks, a.drain, a.seed)
-        res.append({"rate": rate, "server": srv, "plain": plain})
+        srv = _serve_run(pool, rate, a.duration, a.kicks, a.drain, a.seed, a.max_large)
+        plain = (_plain_run(pool, rate, a.duration, a.kicks, a.drain, a.seed)
+                 if a.plain else None)
+        res.append({"rate": rate, "max_large": a.max_large, "server": srv, "plain": plain})
     print(json.dumps({"workload": f"serving: Poisson arrivals, n log-uniform "
                                   f"[{a.n_lo},{a.n_hi}], clustered/uniform 50/50, NN start, "
                                   f"descent + {a.kicks} kicks",
@@ -245,6 +295,11 @@ def main():
     p.add_argument("--n-lo", type=int, default=100)
     p.add_argument("--n-hi", type=int, default=20000)
     p.add_argument("--sizes", default="10000,100000,1000000")
+    p.add_argument("--max-large", type=int, default=0,
+                   help="serve: requests above the batch limit in flight (0 = default)")
+    p.add_argument("--plain", type=int, default=1, help="serve: also time the plain path")
+    p.add_argument("--characterize", type=int, default=0,
+                   help="serve: first run every pool instance once and report its work")
     a = p.parse_args()
     if a.kicks is None:
         a.kicks = {"large": 1000, "serve": 50}.get(a.cmd, 0)

@@ -165,7 +165,8 @@ SWEEP_KERNELS = {0: ("sweep_kernel", "MUFU screen"),
                  1: ("sweep_kernel2", "packed MUFU screen"),
                  2: ("sweep_kernel3", "square-root-free screen"),
                  3: ("sweep_kernel4", "packed square-root-free screen"),
-                 4: ("sweep_kernel5", "fused two-stage square-root-free screen")}
+                 4: ("sweep_kernel5", "fused two-stage square-root-free screen"),
+                 5: ("sweep_kernel6", "local-coordinate expanded screen")}
 
 
 def profile_traffic(kernel):

@@ -385,17 +385,23 @@ logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per
  * LOGO_SWEEP_FUSED: two-stage squared screen with the window threshold
  *   folded into the sum of squares: d(i, c) for every pair (FADD2/FFMA2, two
  *   rows at a time), d(i-1, c-1) only where that passes; threads share the
- *   best delta found so far within a sweep. */
+ *   best delta found so far within a sweep.
+ * LOGO_SWEEP_LOCAL: the test on d(i, c) expanded in coordinates relative to
+ *   the tile's first row, |q|^2 - 2 r.q against a per-row threshold with a
+ *   proven rounding margin (two FFMA per pair), then the fused screen's
+ *   remaining stages. */
 #define LOGO_SWEEP_MUFU 0
 #define LOGO_SWEEP_MUFU_PACKED 1
 #define LOGO_SWEEP_SQUARED 2
 #define LOGO_SWEEP_SQUARED_PACKED 3
 #define LOGO_SWEEP_FUSED 4
+#define LOGO_SWEEP_LOCAL 5
 /* Selects variant and tile shape together (logo_ctx_set_shape keeps the
  * variant).  Shapes per variant: SQUARED (R,NW) in {(2,2),(4,2),(4,4),(8,4),
  * (8,8),(16,4)}; MUFU {(2,2),(2,4),(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)};
- * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED and
- * FUSED {(4,4),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096. */
+ * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED
+ * {(4,4),(8,4),(8,8),(16,4)}; FUSED {(4,2),(4,4),(4,8),(8,2),(8,4),(8,8),(16,4)};
+ * LOCAL {(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096. */
 logo_status logo_ctx_set_kernel(logo_ctx *ctx, int variant, int rows_per_thread,
                                 int warps_per_cta, uint32_t tile_cols);
 

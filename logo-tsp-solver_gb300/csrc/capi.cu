@@ -105,24 +105,21 @@ uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) /
 // Default tile shape by size (overridable through logo_ctx_set_shape and
 // logo_ctx_set_kernel).
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
-    // measured on GB300 (one sweep): from n = 15k up the fused two-stage
-    // screen is fastest (n = 100k NN tour: 0.90 ms vs 1.16 ms for the packed
-    // squared screen and 1.72 ms MUFU; n = 20k NN tour: 0.069 ms vs 0.084 MUFU;
-    // n = 1M random tour: 80.6 ms with 8-row blocks and 1024-column tiles vs
-    // 105.6 and 170.2); below that the MUFU screen, whose test is tighter on
-    // short tours, wins (n = 10k NN tour: 0.042 ms vs 0.059 ms).
+    // measured on GB300 (one sweep): from n = 15k up the local-coordinate
+    // screen is fastest (n = 100k NN tour: 0.633 ms vs 0.834 ms for the fused
+    // screen, 1.16 ms for the packed squared screen and 1.72 ms MUFU; n = 20k
+    // NN tour: 0.061 ms vs 0.068 fused and 0.084 MUFU; n = 1M random tour:
+    // 54.6 ms vs 70.9 fused); below that the MUFU screen, whose test is
+    // tighter on short tours, wins (n = 10k NN tour: 0.040 ms vs 0.057 ms).
     variant = LOGO_SWEEP_MUFU;
-    if (n >= 500000) {
-        variant = LOGO_SWEEP_FUSED;
-        R = 8; NW = 4; cb = 1024;
-    } else if (n >= 60000) {
-        variant = LOGO_SWEEP_FUSED;
+    if (n >= 60000) {
+        variant = LOGO_SWEEP_LOCAL;
         R = 4; NW = 4; cb = 512;
     } else if (n >= 30000) {
-        variant = LOGO_SWEEP_FUSED;
+        variant = LOGO_SWEEP_LOCAL;
         R = 4; NW = 4; cb = 256;
     } else if (n >= 15000) {
-        variant = LOGO_SWEEP_FUSED;
+        variant = LOGO_SWEEP_LOCAL;
         R = 4; NW = 4; cb = 128;
     } else if (n >= 3000) {
         R = 4; NW = 4; cb = 128;
@@ -466,7 +463,7 @@ logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
 
 logo_status logo_ctx_set_kernel(logo_ctx* c, int variant, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
-    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_FUSED)
+    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_LOCAL)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown sweep variant");
     if (!sweep_shape_supported(R, NW, variant) || cb < 16 || cb > 4096)
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape for this variant");

@@ -17,7 +17,7 @@ struct SweepLaunch {
     uint32_t ntiles;
     uint32_t cb;         // columns per tile
     int R, NW;           // rows per thread, warps per CTA
-    int variant;         // LOGO_SWEEP_* (0 MUFU, 1 MUFU f32x2, 2 squared, 3 squared f32x2, 4 fused)
+    int variant;         // LOGO_SWEEP_* (0 MUFU, 1 MUFU f32x2, 2 squared, 3 squared f32x2, 4 fused, 5 local)
     float margin;        // filter margin M
     DevState* st;
 };

@@ -31,6 +31,7 @@
 #include "sweep_core3.cuh"
 #include "sweep_core4.cuh"
 #include "sweep_core5.cuh"
+#include "sweep_core6.cuh"
 
 namespace logo {
 
@@ -297,6 +298,89 @@ __global__ void __launch_bounds__(NW * 32)
     if (lane == 0 && best != kNoMove) atomicMin(&st->best_key, (unsigned long long)best);
 }
 
+// Local-coordinate expanded variant (sweep_core6.cuh): the staged tile stays
+// in shared memory for stages 2 and 3, beside three float arrays (p, q, C of
+// every column relative to the tile's origin, read as float4 by stage 1) and
+// the largest edge of every 32-column window.
+__host__ __device__ constexpr size_t sweep6_cols4(uint32_t cb) { return (cb + 3) & ~(size_t)3; }
+__host__ __device__ constexpr size_t sweep6_cx_offset(uint32_t cb) {
+    return 96 + (size_t)(cb + 1) * sizeof(OrderedCity);
+}
+__host__ __device__ constexpr size_t sweep6_wmax_offset(uint32_t cb) {
+    return sweep6_cx_offset(cb) + 3 * sweep6_cols4(cb) * sizeof(float);
+}
+
+template <int R, int NW, int G>
+__global__ void __launch_bounds__(NW * 32)
+    sweep_kernel6(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
+                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, DevState* st) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
+    float* cx = reinterpret_cast<float*>(smem_raw + sweep6_cx_offset(cb));
+    float* cy = cx + sweep6_cols4(cb);
+    float* cc = cy + sweep6_cols4(cb);
+    float* wmax = reinterpret_cast<float*>(smem_raw + sweep6_wmax_offset(cb));
+
+    if (*(volatile unsigned int*)&st->converged) return;
+    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
+    const uint2 tile = tiles[blockIdx.x];
+    const uint32_t row0 = tile.x, col0 = tile.y;
+    const uint32_t col_end = min(col0 + cb, n);
+    const uint32_t ncols = col_end - col0 + 1;
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = ncols * (uint32_t)sizeof(OrderedCity);
+        mbar_arrive_expect_tx(bar, bytes);
+        bulk_g2s(stage, Q + (col0 - 1), bytes, bar);
+    }
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t ib = row0 + (warp * 32 + lane) * R;
+    Best5 bs;
+    bs.best = kNoMove;
+    bs.B = -1;
+    {
+        const uint64_t gk = *(volatile unsigned long long*)&st->best_key;
+        if (gk != kNoMove) bs.B = min(bs.B, key_delta(gk));
+    }
+    bs.G = bs.B;
+    bs.busy = false;
+    const OrderedCity origin = Q[row0];  // same for every thread of the tile
+    RowBlock6<R> rb;
+    load_rows6<R>(rb, Q, ib, n, origin.x, origin.y);
+    refresh6<R>(rb, Q, ib, n, bs.B);
+    const bool staged = mbar_wait_bounded(bar, 0, &st->status);
+    const uint32_t nwin = (col_end - col0 + kWin6 - 1) / kWin6;
+    if (staged) {
+        for (uint32_t k = threadIdx.x + 1; k < ncols; k += NW * 32) {
+            const OrderedCity q = stage[k];
+            const float p = __fsub_rn(q.x, origin.x), qq = __fsub_rn(q.y, origin.y);
+            cx[k - 1] = p;
+            cy[k - 1] = qq;
+            cc[k - 1] = __fmaf_rn(qq, qq, __fmul_rn(p, p));
+        }
+        for (uint32_t w = threadIdx.x; w < nwin; w += NW * 32) {
+            const uint32_t a = 1 + w * kWin6, b = min(a + kWin6, ncols);
+            float m = 0.f;
+            for (uint32_t k = a; k < b; ++k) m = fmaxf(m, stage[k].e);
+            wmax[w] = m;
+        }
+    }
+    __syncthreads();
+    if (staged) {
+        const ColTile6 t{cx, cy, cc, stage};
+        walk_columns6<R, G>(rb, t, wmax, col0, col0, col_end, ib, n, st, bs);
+    }
+
+    const uint64_t best = warp_min_u64(bs.best);
+    if (lane == 0 && best != kNoMove) atomicMin(&st->best_key, (unsigned long long)best);
+}
+
 __host__ __device__ constexpr size_t sweep2_cols_offset(uint32_t cb) {
     return (96 + (size_t)(cb + 1) * sizeof(OrderedCity) + 31) & ~(size_t)31;
 }
@@ -426,6 +510,34 @@ static cudaError_t launch_sweep5_t(const SweepLaunch& L, cudaStream_t s, bool pr
                                    : launch_sweep5_g<R, NW, 1>(L, s, false);
 }
 
+size_t sweep6_smem_bytes(uint32_t cb) {
+    return sweep6_wmax_offset(cb) + ((size_t)cb / kWin6 + 2) * sizeof(float);
+}
+
+template <int R, int NW, int G>
+static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool prepare) {
+    const size_t smem = sweep6_smem_bytes(L.cb);
+    if (prepare) {
+        return cudaFuncSetAttribute(sweep_kernel6<R, NW, G>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+    }
+    sweep_kernel6<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
+                                                           L.st);
+    return cudaGetLastError();
+}
+
+template <int R, int NW>
+static cudaError_t launch_sweep6_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
+    constexpr int G = 64 / R;
+    if (prepare) {
+        const cudaError_t e = launch_sweep6_g<R, NW, 4>(L, s, true);
+        return e != cudaSuccess ? e : launch_sweep6_g<R, NW, G>(L, s, true);
+    }
+    return L.n >= kSweep5GroupMinN ? launch_sweep6_g<R, NW, G>(L, s, false)
+                                   : launch_sweep6_g<R, NW, 4>(L, s, false);
+}
+
 template <int R, int NW>
 static cudaError_t launch_sweep3_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     const size_t smem = sweep_smem_bytes(L.cb);
@@ -453,6 +565,17 @@ static cudaError_t launch_sweep_t(const SweepLaunch& L, cudaStream_t s, bool pre
 }
 
 static cudaError_t dispatch_sweep(const SweepLaunch& L, cudaStream_t s, bool prepare) {
+    if (L.variant == 5) {
+        switch (L.R * 100 + L.NW) {
+            case 402: return launch_sweep6_t<4, 2>(L, s, prepare);
+            case 404: return launch_sweep6_t<4, 4>(L, s, prepare);
+            case 408: return launch_sweep6_t<4, 8>(L, s, prepare);
+            case 804: return launch_sweep6_t<8, 4>(L, s, prepare);
+            case 808: return launch_sweep6_t<8, 8>(L, s, prepare);
+            case 1604: return launch_sweep6_t<16, 4>(L, s, prepare);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     if (L.variant == 4) {
         switch (L.R * 100 + L.NW) {
             case 402: return launch_sweep5_t<4, 2>(L, s, prepare);
@@ -519,6 +642,14 @@ cudaError_t launch_sweep_prepare(const SweepLaunch& L) {
 }
 
 bool sweep_shape_supported(int R, int NW, int variant) {
+    if (variant == 5) {
+        switch (R * 100 + NW) {
+            case 402: case 404: case 408: case 804: case 808: case 1604:
+                return true;
+            default:
+                return false;
+        }
+    }
     if (variant == 4) {
         switch (R * 100 + NW) {
             case 402: case 404: case 408: case 802: case 804: case 808: case 1604:

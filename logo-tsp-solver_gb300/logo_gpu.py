@@ -26,6 +26,7 @@ SWEEP_MUFU_PACKED = 1
 SWEEP_SQUARED = 2
 SWEEP_SQUARED_PACKED = 3
 SWEEP_FUSED = 4
+SWEEP_LOCAL = 5
 MAX_CITIES = 2097152
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",
@@ -339,7 +340,7 @@ class Solver:
         return {k: getattr(i, k) for k, _ in CtxInfo._fields_}
 
     def set_kernel(self, variant, rows_per_thread, warps_per_cta, tile_cols):
-        """Variant (SWEEP_MUFU .. SWEEP_FUSED) and tile shape."""
+        """Variant (SWEEP_MUFU .. SWEEP_LOCAL) and tile shape."""
         _check(load().logo_ctx_set_kernel(self._h, variant, rows_per_thread, warps_per_cta,
                                           tile_cols), self._h)
 

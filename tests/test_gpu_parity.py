@@ -60,7 +60,9 @@ KERNELS = [(2, 2, 2, 64), (2, 4, 2, 128), (2, 4, 4, 64), (2, 8, 4, 1024), (2, 8,
            (1, 16, 4, 1024),
            (3, 4, 4, 64), (3, 8, 4, 512), (3, 8, 8, 100), (3, 16, 4, 1024),
            (4, 4, 2, 64), (4, 4, 4, 64), (4, 4, 8, 256), (4, 8, 2, 128), (4, 8, 4, 512),
-           (4, 8, 8, 100), (4, 16, 4, 1024)]
+           (4, 8, 8, 100), (4, 16, 4, 1024),
+           (5, 4, 2, 64), (5, 4, 4, 64), (5, 4, 8, 256), (5, 8, 4, 512), (5, 8, 8, 100),
+           (5, 16, 4, 1024)]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -83,7 +85,7 @@ def test_every_tile_shape(lg, inst, oracle_mod, kernel):
             assert np.array_equal(got, want), kernel
 
 
-VARIANTS = [(v, 8, 4, 128) for v in range(5)]
+VARIANTS = [(v, 8, 4, 128) for v in range(6)]
 
 
 @pytest.mark.parametrize("kernel", VARIANTS)
@@ -219,13 +221,15 @@ def test_sqrt_error_bound(lg):
     assert 0 < err <= 2.0 ** -23, err
 
 
-FUSED_SHAPES = [(4, 4, 256), (4, 2, 256), (4, 8, 128), (8, 4, 512), (8, 8, 256), (16, 4, 1024)]
+GROUPED_KERNELS = [(4, 4, 4, 256), (4, 4, 2, 256), (4, 4, 8, 128), (4, 8, 4, 512), (4, 8, 8, 256),
+                   (4, 16, 4, 1024), (5, 4, 4, 256), (5, 4, 2, 256), (5, 4, 8, 128),
+                   (5, 8, 4, 512), (5, 8, 8, 256), (5, 16, 4, 1024)]
 
 
-def test_fused_grouped_path_late_descent(lg, inst, oracle_mod):
-    """n = 40,000 (the fused screen's grouped column walk): the NN start tour
-    and states late in its descent (small deltas, tight screens) choose the
-    oracle's move with every fused tile shape."""
+def test_grouped_paths_late_descent(lg, inst, oracle_mod):
+    """n = 40,000 (the grouped column walks of the fused and local-coordinate
+    screens): the NN start tour and states late in its descent (small deltas,
+    tight screens) choose the oracle's move with every tile shape."""
     n = 40000
     xy = inst.clustered(n, 21, side=1.0e6, clusters=80, sigma_frac=0.01)
     r0, _ = oracle_mod.nn_tour(xy)
@@ -238,17 +242,19 @@ def test_fused_grouped_path_late_descent(lg, inst, oracle_mod):
             for r in states]
     assert want[1][0] == 0 and want[2][0] < 0
     with lg.Solver(xy) as s:
-        for R, NW, cb in FUSED_SHAPES:
-            s.set_kernel(lg.SWEEP_FUSED, R, NW, cb)
+        for kernel in GROUPED_KERNELS:
+            s.set_kernel(*kernel)
             for k, r in enumerate(states):
-                assert s.optimize_step(r) == want[k], ((R, NW, cb), k)
+                assert s.optimize_step(r) == want[k], (kernel, k)
 
 
 @pytest.mark.parametrize("n,gen,variant", [(100000, "clustered_nn", None),
                                            (100000, "clustered_nn", 2),
                                            (100000, "clustered_nn", 4),
+                                           (100000, "clustered_nn", 5),
                                            (200000, "uniform_random", None),
-                                           (200000, "uniform_random", 4)])
+                                           (200000, "uniform_random", 4),
+                                           (200000, "uniform_random", 5)])
 def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen, variant):
     """Full-size single sweeps against the oracle's multi-threaded sweep
     (default kernel and the square-root-free screens)."""

@@ -48,12 +48,14 @@ struct DevState {
     unsigned long long best_length; // ILS best
     unsigned long long accepted;
     unsigned long long kicks;
+    unsigned long long sweeps_at_reset;  // sweeps when the current descent began
     unsigned int cur;               // which buffer holds the tour
     unsigned int converged;
     unsigned int status;            // kErr* bits
     unsigned int done_blocks;       // last-block-done counter
     unsigned int log_cap;
     unsigned int len_done;          // last-block counter of the length sum
+    unsigned int bad_route;         // set by the gather: the route is not a permutation
     int* move_log;                  // (delta, i, j) per move, or null
     unsigned long long length_acc;  // partial sums of tour_length_kernel
 };

@@ -36,8 +36,11 @@ struct TourBufs {
     const float2* xy;
     uint32_t n;
     DevState* st;
+    uint32_t* seen;  // (n + 31) / 32 words, zero before launch_init_ordered
 };
-// Builds Q[0] from xy and route[0] (route already uploaded to route[0]).
+// Builds Q[0] from xy and route[0] (route already uploaded to route[0]) and
+// checks that route[0] is a permutation of 0..n-1 (st->bad_route = 1 if not;
+// out-of-range entries are read as city 0).
 cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s);
 // Prepares *st for a new descent: cur = 0 kept, counters cleared.
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,

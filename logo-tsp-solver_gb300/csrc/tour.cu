@@ -46,11 +46,19 @@ __device__ __forceinline__ bool last_block_done(unsigned int* counter) {
 
 __global__ void init_ordered_kernel(const float2* __restrict__ xy,
                                     const uint32_t* __restrict__ route,
-                                    OrderedCity* __restrict__ Q, uint32_t n) {
+                                    OrderedCity* __restrict__ Q, uint32_t n,
+                                    uint32_t* __restrict__ seen, DevState* st) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x) {
-        const float2 a = xy[route[k]];
-        const float2 b = xy[route[k == 0 ? n - 1 : k - 1]];
+        uint32_t v = route[k], w = route[k == 0 ? n - 1 : k - 1];
+        // permutation check: each city marks its bit once
+        bool bad = v >= n;
+        if (!bad) bad = atomicOr(&seen[v >> 5], 1u << (v & 31)) & (1u << (v & 31));
+        if (bad) st->bad_route = 1u;
+        v = v < n ? v : 0u;
+        w = w < n ? w : 0u;
+        const float2 a = xy[v];
+        const float2 b = xy[w];
         OrderedCity o;
         o.x = a.x;
         o.y = a.y;
@@ -63,7 +71,8 @@ __global__ void init_ordered_kernel(const float2* __restrict__ xy,
 __global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves) {
     st->best_key = kNoMove;
     st->moves = 0;
-    st->converged = 0;
+    st->converged = st->bad_route ? 1u : 0u;  // nothing to descend on a bad route
+    st->sweeps_at_reset = st->sweeps;
     st->done_blocks = 0;
     st->max_moves = max_moves;
 }
@@ -232,7 +241,8 @@ __global__ void save_best_kernel(TourBufs T) {
 }  // namespace
 
 cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s) {
-    init_ordered_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, T.route[0], T.Q[0], T.n);
+    init_ordered_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, T.route[0], T.Q[0], T.n,
+                                                           T.seen, T.st);
     return cudaGetLastError();
 }
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,

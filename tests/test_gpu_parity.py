@@ -214,6 +214,36 @@ def test_invalid_arguments(lg, inst):
         lg.Solver(far)
 
 
+def test_bad_routes_rejected_then_context_usable(lg, inst, oracle_mod):
+    """The route check runs on the device: a duplicate or out-of-range entry
+    makes every entry point return INVALID_ARG, drops the resident route, and
+    the next valid route works as usual."""
+    n = 5000
+    xy = inst.uniform_f32(n, 9, 1.0e6)
+    r = inst.random_tour(n, 9)
+    dup = r.copy()
+    dup[n - 1] = dup[0]
+    oor = r.copy()
+    oor[1234] = n
+    with lg.Solver(xy) as s:
+        for bad in (dup, oor):
+            for call in (s.optimize_step, s.optimize, s.route_length, s.set_route,
+                         lambda b: s.ils(b, 2, 1, lg.KICK_SEGMENT)):
+                with pytest.raises(lg.LogoError) as e:
+                    call(bad)
+                assert e.value.status == 1
+            with pytest.raises(lg.LogoError):
+                s.get_route()
+        assert s.optimize_step(r) == oracle_mod.best_move(xy, r)
+        assert s.route_length(r) == oracle_mod.tour_length(xy, r)
+        got, st = s.optimize(r, max_moves=3)
+        want = r.copy()
+        for _ in range(3):
+            d, i, j = oracle_mod.best_move(xy, want)
+            want = oracle_mod.apply_move(want, i, j)
+        assert np.array_equal(got, want) and st["moves"] == 3
+
+
 def test_sqrt_error_bound(lg):
     """The filter margin assumes the approximate sqrt is within 2^-20
     relative; require 8x headroom over what the hardware actually does."""

@@ -364,6 +364,8 @@ typedef struct logo_ctx_info {
     float filter_margin;  /* bound on |exact - approximate delta| */
     uint32_t graph_steps; /* sweep+apply steps per graph launch */
     int variant;          /* LOGO_SWEEP_* */
+    int descent_mode;     /* LOGO_DESCENT_* in use */
+    int cooperative_ctas; /* CTAs of the cooperative descent; 0 if unavailable */
 } logo_ctx_info;
 
 logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
@@ -372,6 +374,20 @@ logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
  * tile); used by the autotuner.  Invalid shapes return INVALID_ARG. */
 logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per_cta,
                                uint32_t tile_cols);
+
+/* How a descent is driven; all modes return identical moves.
+ * LOGO_DESCENT_AUTO (default): COOPERATIVE where available, else GRAPH.
+ * LOGO_DESCENT_GRAPH: captured CUDA graphs of (sweep, gather) launches,
+ *   replayed until the device convergence flag is set.
+ * LOGO_DESCENT_COOPERATIVE: one cooperative persistent launch per descent
+ *   (tours of 8 to 6,144 cities, held in every CTA's shared memory; one
+ *   grid barrier per move).  No counterpart in the reference, whose descent is a
+ *   host loop over optimizeStep (src/solvers/twoOptLocalSolver.cpp:22-64). */
+#define LOGO_DESCENT_AUTO 0
+#define LOGO_DESCENT_GRAPH 1
+#define LOGO_DESCENT_COOPERATIVE 2
+/* INVALID_ARG for an unknown mode, or COOPERATIVE where it is unavailable. */
+logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
 
 /* Sweep kernel variants; all return identical moves (the default depends on
  * n, see logo_ctx_info.variant).

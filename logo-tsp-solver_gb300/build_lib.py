@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblogo_gpu.so")
-SOURCES = ["sweep.cu", "tour.cu", "capi.cu", "diag.cu", "construct.cpp", "batch.cu",
+SOURCES = ["sweep.cu", "tour.cu", "coop.cu", "capi.cu", "diag.cu", "construct.cpp", "batch.cu",
            "capi_batch.cu", "noalloc.cu",
            "serve.cu", "capi_server.cu"]
 # host files whose floating point must not be contracted into FMAs

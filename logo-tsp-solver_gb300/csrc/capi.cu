@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -34,6 +35,9 @@ struct logo_ctx {
     DevState* h_st = nullptr;  // pinned mirror
     uint32_t* h_route = nullptr;  // pinned staging
     uint32_t* d_seen = nullptr;   // bitmap of the route permutation check
+    CoopSync* d_coop = nullptr;   // barrier and best-key slots of the cooperative descent
+    int coop_grid = 0;            // CTAs of the cooperative descent (0: unavailable)
+    int descent_mode = LOGO_DESCENT_AUTO;
     uint2* d_tiles = nullptr;
     uint32_t ntiles = 0;
     int R = 8, NW = 4;
@@ -107,24 +111,28 @@ uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) /
 // Default tile shape by size (overridable through logo_ctx_set_shape and
 // logo_ctx_set_kernel).
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
-    // measured on GB300 (one sweep): from n = 15k up the local-coordinate
-    // screen is fastest (n = 100k NN tour: 0.633 ms vs 0.834 ms for the fused
-    // screen, 1.16 ms for the packed squared screen and 1.72 ms MUFU; n = 20k
-    // NN tour: 0.061 ms vs 0.068 fused and 0.084 MUFU; n = 1M random tour:
-    // 54.6 ms vs 70.9 fused); below that the MUFU screen, whose test is
-    // tighter on short tours, wins (n = 10k NN tour: 0.040 ms vs 0.057 ms).
+    // measured on GB300 (one sweep, NN start tours and states 5% into their
+    // descents): from n = 17.5k up the local-coordinate screen is fastest
+    // (n = 100k: 0.633 ms vs 0.834 ms fused, 1.16 ms packed squared, 1.72 ms
+    // MUFU; n = 20k: 0.070 ms with 64-column tiles vs 0.083 MUFU; n = 1M random
+    // tour: 54.6 ms vs 70.9 fused); below it the MUFU screen, whose test is
+    // tighter on short tours, wins, with 64-column tiles from 3k (n = 10k:
+    // 0.030 ms vs 0.042 with (4, 4, 128) tiles; n = 15k: 0.052 vs 0.060 local).
     variant = LOGO_SWEEP_MUFU;
     if (n >= 60000) {
         variant = LOGO_SWEEP_LOCAL;
         R = 4; NW = 4; cb = 512;
-    } else if (n >= 30000) {
+    } else if (n >= 45000) {
         variant = LOGO_SWEEP_LOCAL;
         R = 4; NW = 4; cb = 256;
-    } else if (n >= 15000) {
+    } else if (n >= 30000) {
         variant = LOGO_SWEEP_LOCAL;
         R = 4; NW = 4; cb = 128;
+    } else if (n >= 17500) {
+        variant = LOGO_SWEEP_LOCAL;
+        R = 4; NW = 4; cb = 64;
     } else if (n >= 3000) {
-        R = 4; NW = 4; cb = 128;
+        R = 4; NW = 2; cb = 64;
     } else {
         R = 2; NW = 2; cb = 64;
     }
@@ -242,6 +250,21 @@ logo_status status_to_error(logo_ctx* c, unsigned int st) {
 
 // Descent on the resident tour.  Replays the chunk graph until the device
 // reports convergence (or the move limit).
+logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0);
+
+// Cooperative descents of this library never overlap on one device: each
+// grid is sized to be resident on its own, and two whose CTAs were only
+// partly resident would wait on each other's SMs until their barriers gave
+// up.  The lock is held from the launch to its completion.
+std::mutex& coop_lock(int device) {
+    static std::mutex locks[64];
+    return locks[(unsigned)device % 64];
+}
+
+bool use_coop(const logo_ctx* c) {
+    return c->coop_grid > 0 && c->descent_mode != LOGO_DESCENT_GRAPH;
+}
+
 logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
                         uint64_t* sweeps_out, bool reset = true) {
     if (max_moves == 0) max_moves = ~0ull >> 1;
@@ -256,6 +279,43 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
         moves0 = c->h_st->moves;
         sweeps0 = c->h_st->sweeps;
     }
+    if (use_coop(c)) {
+        // one cooperative launch runs the whole descent
+        CK(c, cudaMemsetAsync(c->d_coop, 0xFF, sizeof(CoopSync), c->stream));
+        CK(c, cudaMemsetAsync(c->d_coop, 0, 2 * sizeof(unsigned int), c->stream));
+        CoopArgs A;
+        A.Q0 = c->d_Q[0];
+        A.Q1 = c->d_Q[1];
+        A.R0 = c->d_route[0];
+        A.R1 = c->d_route[1];
+        A.n = c->n;
+        A.margin = c->margin;
+        A.st = c->d_st;
+        A.cs = c->d_coop;
+        logo_status s;
+        {
+            std::lock_guard<std::mutex> lk(coop_lock(c->device));
+            CK(c, launch_coop_descent(A, c->coop_grid, c->stream));
+            s = read_state(c);
+        }
+        if (s != LOGO_OK) return s;
+        if (!c->h_st->converged && !c->h_st->status)
+            return fail(c, LOGO_ERR_DEVICE_FAULT, "cooperative descent did not finish");
+    } else {
+        logo_status s = graph_descent(c, max_moves, reset, moves0);
+        if (s != LOGO_OK) return s;
+    }
+    if (moves_out) *moves_out = c->h_st->moves - moves0;
+    if (sweeps_out)
+        *sweeps_out = c->h_st->sweeps - (reset ? c->h_st->sweeps_at_reset : sweeps0);
+    const unsigned int st = c->h_st->status & ~kErrMoveLimit;
+    if (st) return status_to_error(c, st);
+    return LOGO_OK;
+}
+
+// Replays the chunk graph (or single steps when fewer moves are allowed than
+// a chunk holds) until the device flags convergence.
+logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0) {
     uint64_t before = moves0;
     for (;;) {
         const uint64_t left = max_moves - (before - moves0);
@@ -278,11 +338,6 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
             return fail(c, LOGO_ERR_DEVICE_FAULT, "descent made no progress");
         before = c->h_st->moves;
     }
-    if (moves_out) *moves_out = c->h_st->moves - moves0;
-    if (sweeps_out)
-        *sweeps_out = c->h_st->sweeps - (reset ? c->h_st->sweeps_at_reset : sweeps0);
-    const unsigned int st = c->h_st->status & ~kErrMoveLimit;
-    if (st) return status_to_error(c, st);
     return LOGO_OK;
 }
 
@@ -318,6 +373,7 @@ void destroy(logo_ctx* c) {
     cudaFree(c->d_st);
     cudaFree(c->d_tiles);
     cudaFree(c->d_seen);
+    cudaFree(c->d_coop);
     if (c->h_st) cudaFreeHost(c->h_st);
     if (c->h_route) cudaFreeHost(c->h_route);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -433,6 +489,8 @@ logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_
     CKC(cudaMallocHost(&c->h_st, sizeof(DevState)));
     CKC(cudaMallocHost(&c->h_route, sizeof(uint32_t) * n));
     CKC(cudaMalloc(&c->d_seen, sizeof(uint32_t) * ((n + 31) / 32)));
+    c->coop_grid = coop_grid(n, device);
+    if (c->coop_grid > 0) CKC(cudaMalloc(&c->d_coop, sizeof(CoopSync)));
     std::memset(c->h_st, 0, sizeof(DevState));
     c->h_st->best_key = kNoMove;
     c->h_st->converged = 1;
@@ -461,6 +519,20 @@ logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
     info->filter_margin = c->margin;
     info->graph_steps = c->chunk_steps;
     info->variant = c->variant;
+    info->descent_mode = use_coop(c) ? LOGO_DESCENT_COOPERATIVE : LOGO_DESCENT_GRAPH;
+    info->cooperative_ctas = c->coop_grid;
+    return LOGO_OK;
+}
+
+logo_status logo_ctx_set_descent_mode(logo_ctx* c, int mode) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (mode != LOGO_DESCENT_AUTO && mode != LOGO_DESCENT_GRAPH &&
+        mode != LOGO_DESCENT_COOPERATIVE)
+        return fail(c, LOGO_ERR_INVALID_ARG, "unknown descent mode");
+    if (mode == LOGO_DESCENT_COOPERATIVE && c->coop_grid <= 0)
+        return fail(c, LOGO_ERR_INVALID_ARG,
+                    "cooperative descent unavailable (n above 6,144 or device without it)");
+    c->descent_mode = mode;
     return LOGO_OK;
 }
 

@@ -1,0 +1,282 @@
+// Cooperative persistent descent for small tours (n <= kCoopMaxN = 6,144),
+// sm_103a.
+//
+// The multi-kernel descent launches a sweep and a gather per move; for small
+// and mid-size tours those two launches (10 us and 5 us at n = 1000) are
+// mostly latency, not work.  Here one cooperative launch runs the whole
+// descent: every CTA holds the ordered tour (x, y, incoming edge, city id in
+// the spare field) in its own shared memory, the CTAs' warps share the
+// sweep's warp tiles (sweep_core.cuh, MUFU screen, exact re-evaluation), the
+// per-CTA best keys meet in one 64-bit atomicMin per move, and after one grid
+// barrier every CTA reads the same best move and applies it to its own copy
+// (rotate + reverse in place: rev[p,q) || rev[q,n), then rev[0,q), as in
+// cta_tour.cuh).  Per move: one barrier, no global tour traffic.
+//
+// Move semantics, candidate set, tie rule and the DevState bookkeeping are
+// those of sweep.cu + apply_move_kernel (src/solvers/twoOptLocalSolver.cpp:
+// 22-64): moves, total_moves, sweeps (+1 for the converging sweep), the move
+// log, kErrMoveLimit at max_moves, kErrBadKey on an out-of-range key.  The
+// final tour is written back to buffer `cur` by CTA 0.
+//
+// Best-key slots rotate over three entries: move m uses slot m % 3, and
+// before arriving at barrier m CTA 0 clears slot (m + 1) % 3, which every CTA
+// finished reading before it arrived at barrier m - 1.  Barrier waits are
+// bounded (2 s of %globaltimer); a CTA that gives up sets kErrTimeout and
+// leaves the loop, so the others give up too and the launch ends.
+#include "logo_device.cuh"
+#include "logo_internal.h"
+#include "sweep_core.cuh"
+
+namespace logo {
+
+namespace {
+
+constexpr unsigned long long kCoopWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned int* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier (generation counter); false when the wait ran out.
+__device__ bool grid_barrier(CoopSync* cs, unsigned int nblocks, DevState* st, bool* ok_s) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int g = ld_acquire_u32(&cs->gen);
+        __threadfence();
+        const unsigned int t = atomicAdd(&cs->count, 1u);
+        bool ok = true;
+        if (t == nblocks - 1) {
+            atomicExch(&cs->count, 0u);
+            __threadfence();
+            atomicAdd(&cs->gen, 1u);
+        } else {
+            const unsigned long long t0 = global_timer_ns();
+            while (ld_acquire_u32(&cs->gen) == g) {
+                if (global_timer_ns() - t0 > kCoopWaitNs) {
+                    atomicOr(&st->status, kErrTimeout);
+                    ok = false;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        *ok_s = ok;
+    }
+    __syncthreads();
+    return *ok_s;
+}
+
+// Reverses [a0, a1) and [b0, b1) (disjoint) of the shared tour in one pass.
+template <int NT>
+__device__ __forceinline__ void reverse2_f4(float4* T, uint32_t a0, uint32_t a1, uint32_t b0,
+                                            uint32_t b1) {
+    const uint32_t ha = (a1 - a0) / 2, hb = (b1 - b0) / 2;
+    for (uint32_t t = threadIdx.x; t < ha + hb; t += NT) {
+        uint32_t x, y;
+        if (t < ha) {
+            x = a0 + t;
+            y = a1 - 1 - t;
+        } else {
+            x = b0 + (t - ha);
+            y = b1 - 1 - (t - ha);
+        }
+        const float4 vx = T[x], vy = T[y];
+        T[x] = vy;
+        T[y] = vx;
+    }
+}
+
+template <int R, int TC, int NT>
+__global__ void __launch_bounds__(NT) coop_descent_kernel(CoopArgs A) {
+    constexpr int kCoopThreads = NT;
+    constexpr int kCoopWarps = NT / 32;
+    extern __shared__ __align__(16) unsigned char coop_smem[];
+    OrderedCity* Q = reinterpret_cast<OrderedCity*>(coop_smem);
+    const uint32_t n = A.n;
+    uint32_t* tbl = reinterpret_cast<uint32_t*>(coop_smem + (size_t)n * sizeof(OrderedCity));
+    __shared__ unsigned long long wbest[kCoopWarps];
+    __shared__ bool bar_ok;
+    DevState* st = A.st;
+    CoopSync* cs = A.cs;
+    // set before the launch and identical for every CTA
+    if (*(volatile unsigned int*)&st->converged) return;
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    OrderedCity* Qg = cur ? A.Q1 : A.Q0;
+    uint32_t* Rg = cur ? A.R1 : A.R0;
+    for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads) {
+        OrderedCity o = Qg[k];
+        o.pad = __uint_as_float(Rg[k]);
+        Q[k] = o;
+    }
+    constexpr uint32_t RT = 32 * R;
+    const uint32_t nrb = (n - 3 + RT - 1) / RT;  // row blocks over rows 1..n-3
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        tbl[0] = 0;
+        for (uint32_t b = 0; b < nrb; ++b) {
+            const uint32_t row0 = 1 + b * RT;
+            acc += (n - row0 - 2 + TC - 1) / TC;
+            tbl[b + 1] = acc;
+        }
+    }
+    __syncthreads();
+    const uint32_t total = tbl[nrb];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long m0 = *(volatile unsigned long long*)&st->moves;
+    const unsigned long long maxm = *(volatile unsigned long long*)&st->max_moves;
+    unsigned long long m = 0, sweeps = 0;
+    bool limit = false, bad = false, failed = false;
+    for (;;) {
+        // sweep: warp tiles dealt over every warp of the grid
+        uint64_t best = kNoMove;
+        for (uint32_t t = blockIdx.x * kCoopWarps + warp; t < total;
+             t += gridDim.x * kCoopWarps) {
+            uint32_t lo = 0, hi = nrb;  // row block b with tbl[b] <= t < tbl[b + 1]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (tbl[mid] <= t) lo = mid; else hi = mid;
+            }
+            const uint32_t row0 = 1 + lo * RT;
+            const uint32_t col0 = row0 + 2 + (t - tbl[lo]) * TC;
+            const uint32_t col1 = min(col0 + TC, n);
+            const uint32_t ib = row0 + lane * R;
+            int B = -1;
+            if (best != kNoMove) B = min(B, key_delta(best));
+            RowBlock<R> rb;
+            load_rows<R>(rb, Q, ib, n);
+            refresh_thresholds<R>(rb, Q, ib, n, B, A.margin);
+            walk_columns<R>(rb, Q, 0, col0, col1, ib, n, Q, A.margin, B, best);
+        }
+        best = warp_min_u64(best);
+        if (lane == 0) wbest[warp] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long k = wbest[0];
+#pragma unroll
+            for (int w = 1; w < kCoopWarps; ++w) k = wbest[w] < k ? wbest[w] : k;
+            if (k != kNoMove) atomicMin(&cs->slot[m % 3], k);
+            if (blockIdx.x == 0) cs->slot[(m + 1) % 3] = kNoMove;
+        }
+        if (!grid_barrier(cs, gridDim.x, st, &bar_ok)) {
+            failed = true;
+            break;
+        }
+        ++sweeps;
+        const unsigned long long key = ld_acquire_u64(&cs->slot[m % 3]);
+        if (key == kNoMove) break;  // local optimum
+        // reported move (i, j+1): p = i < q = j+1 (twoOptLocalSolver.cpp:41-48)
+        const uint32_t p = key_i(key), q = key_j(key);
+        if (!(p >= 1 && q < n && q >= p + 2)) {
+            bad = true;
+            break;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            int* log = st->move_log;
+            const unsigned long long idx = m0 + m;
+            if (log && idx < st->log_cap) {
+                log[3 * idx + 0] = key_delta(key);
+                log[3 * idx + 1] = (int)p;
+                log[3 * idx + 2] = (int)q;
+            }
+        }
+        // new = old[p..q) ++ rev(old[0..p)) ++ rev(old[q..n))
+        float4* T = reinterpret_cast<float4*>(Q);
+        reverse2_f4<NT>(T, p, q, q, n);
+        __syncthreads();
+        reverse2_f4<NT>(T, 0, q, 0, 0);
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads) {
+            const OrderedCity a = Q[k];
+            const OrderedCity b = Q[k == 0 ? n - 1 : k - 1];
+            Q[k].e = (float)exact_dist(b.x, b.y, a.x, a.y);
+        }
+        __syncthreads();
+        ++m;
+        if (m0 + m >= maxm) {
+            limit = true;
+            break;
+        }
+    }
+    if (blockIdx.x == 0 && !failed) {
+        for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads) {
+            OrderedCity o = Q[k];
+            Rg[k] = __float_as_uint(o.pad);
+            o.pad = 0.f;
+            Qg[k] = o;
+        }
+        if (threadIdx.x == 0) {
+            st->moves = m0 + m;
+            st->total_moves += m;
+            st->sweeps += sweeps;
+            st->best_key = kNoMove;
+            st->converged = 1;
+            if (limit) atomicOr(&st->status, kErrMoveLimit);
+            if (bad) atomicOr(&st->status, kErrBadKey);
+        }
+    }
+}
+
+template <int R, int TC>
+size_t coop_smem(uint32_t n) {
+    const uint32_t nrb = (n - 3 + 32 * R - 1) / (32 * R);
+    return (size_t)n * sizeof(OrderedCity) + sizeof(uint32_t) * (nrb + 2);
+}
+
+// Grid for a cooperative launch: every CTA resident at once (occupancy x
+// SMs), and no more CTAs than the sweep has warp tiles for.
+template <int R, int TC, int NT>
+int coop_grid_t(uint32_t n, int device) {
+    const size_t smem = coop_smem<R, TC>(n);
+    if (cudaFuncSetAttribute(coop_descent_kernel<R, TC, NT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return 0;
+    int per_sm = 0, sms = 0, coop = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_descent_kernel<R, TC, NT>,
+                                                      NT, smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess)
+        return 0;
+    if (!coop || per_sm < 1) return 0;
+    constexpr uint32_t RT = 32 * R;
+    uint64_t tiles = 0;
+    for (uint32_t row0 = 1; row0 + 3 <= n; row0 += RT) tiles += (n - row0 - 2 + TC - 1) / TC;
+    const uint64_t want = (tiles + NT / 32 - 1) / (NT / 32);
+    const uint64_t cap = (uint64_t)per_sm * sms;
+    return (int)(want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
+template <int R, int TC, int NT>
+cudaError_t launch_coop_t(const CoopArgs& A, int grid, cudaStream_t s) {
+    CoopArgs a = A;
+    void* args[] = {&a};
+    return cudaLaunchCooperativeKernel((const void*)coop_descent_kernel<R, TC, NT>, dim3(grid),
+                                       dim3(NT), args, coop_smem<R, TC>(A.n), s);
+}
+
+}  // namespace
+
+// Warp tiles of 64 rows x 32 columns; 256-thread CTAs up to 2,500 cities,
+// 512 above (measured on GB300, random tours, microseconds per move: n = 1000
+// 10.4 with 256 threads vs 11.3 with 512, n = 3000 12.7 with 512; the
+// graph-driven descent 16.7 and 29.2; 4-row x 64-column tiles leave most SMs
+// idle at n = 3000, 24.6.  From about 8,000 cities on the graph-driven
+// descent is as fast or faster, so the limit is 6,144).
+int coop_grid(uint32_t n, int device) {
+    if (n < 8 || n > kCoopMaxN) return 0;
+    return n <= 2500 ? coop_grid_t<2, 32, 256>(n, device) : coop_grid_t<2, 32, 512>(n, device);
+}
+
+cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s) {
+    return A.n <= 2500 ? launch_coop_t<2, 32, 256>(A, grid, s)
+                       : launch_coop_t<2, 32, 512>(A, grid, s);
+}
+
+}  // namespace logo

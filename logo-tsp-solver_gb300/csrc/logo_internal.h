@@ -38,6 +38,28 @@ struct TourBufs {
     DevState* st;
     uint32_t* seen;  // (n + 31) / 32 words, zero before launch_init_ordered
 };
+// Cooperative persistent descent (coop.cu) for tours up to kCoopMaxN cities:
+// one launch runs the descent to a local optimum or st->max_moves.
+constexpr uint32_t kCoopMaxN = 6144;
+struct CoopSync {
+    unsigned int count;            // CTAs arrived at the current barrier
+    unsigned int gen;              // barrier generation
+    unsigned long long slot[3];    // best key of move m in slot m % 3
+};
+struct CoopArgs {
+    OrderedCity* Q0;
+    OrderedCity* Q1;
+    uint32_t* R0;
+    uint32_t* R1;
+    uint32_t n;
+    float margin;
+    DevState* st;
+    CoopSync* cs;  // count = gen = 0 and every slot = kNoMove before the launch
+};
+// CTAs for a cooperative launch at this n on `device` (0: not available).
+int coop_grid(uint32_t n, int device);
+cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s);
+
 // Builds Q[0] from xy and route[0] (route already uploaded to route[0]) and
 // checks that route[0] is a permutation of 0..n-1 (st->bad_route = 1 if not;
 // out-of-range entries are read as city 0).

@@ -27,6 +27,9 @@ SWEEP_SQUARED = 2
 SWEEP_SQUARED_PACKED = 3
 SWEEP_FUSED = 4
 SWEEP_LOCAL = 5
+DESCENT_AUTO = 0
+DESCENT_GRAPH = 1
+DESCENT_COOPERATIVE = 2
 MAX_CITIES = 2097152
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",
@@ -43,7 +46,7 @@ EXPORTS = [
     "logo_read_tsplib", "logo_nn_tour", "logo_random_tour", "logo_check_tour",
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
     "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
-    "logo_best_move_noalloc", "logo_ctx_set_kernel",
+    "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
     "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
     "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
 ]
@@ -76,7 +79,8 @@ class CtxInfo(ctypes.Structure):
                 ("rows_per_thread", ctypes.c_int), ("warps_per_cta", ctypes.c_int),
                 ("tile_cols", ctypes.c_uint32), ("tiles", ctypes.c_uint32),
                 ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32),
-                ("variant", ctypes.c_int)]
+                ("variant", ctypes.c_int), ("descent_mode", ctypes.c_int),
+                ("cooperative_ctas", ctypes.c_int)]
 
 
 class Instance(ctypes.Structure):
@@ -165,6 +169,7 @@ def load(path=LIB_PATH):
     L.logo_ctx_get_info.argtypes = [_vp, c.POINTER(CtxInfo)]
     L.logo_ctx_set_shape.argtypes = [_vp, c.c_int, c.c_int, c.c_uint32]
     L.logo_ctx_set_kernel.argtypes = [_vp, c.c_int, c.c_int, c.c_int, c.c_uint32]
+    L.logo_ctx_set_descent_mode.argtypes = [_vp, c.c_int]
     L.logo_ctx_stream.restype = _vp
     L.logo_ctx_stream.argtypes = [_vp]
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
@@ -343,6 +348,10 @@ class Solver:
         """Variant (SWEEP_MUFU .. SWEEP_LOCAL) and tile shape."""
         _check(load().logo_ctx_set_kernel(self._h, variant, rows_per_thread, warps_per_cta,
                                           tile_cols), self._h)
+
+    def set_descent_mode(self, mode):
+        """DESCENT_AUTO, DESCENT_GRAPH or DESCENT_COOPERATIVE."""
+        _check(load().logo_ctx_set_descent_mode(self._h, mode), self._h)
 
     def set_shape(self, rows_per_thread, warps_per_cta, tile_cols):
         _check(load().logo_ctx_set_shape(self._h, rows_per_thread, warps_per_cta, tile_cols),

@@ -106,14 +106,17 @@ def test_every_variant_near_local_optimum(lg, inst, oracle_mod, kernel):
                 assert s.optimize_step(r) == oracle_mod.best_move(xy, r), (kernel, n, k)
 
 
+@pytest.mark.parametrize("mode", ["graph", "cooperative"])
 @pytest.mark.parametrize("seed", [1, 2, 3, 4])
-def test_descent_move_sequence_plain_workload(lg, inst, oracle_mod, seed):
+def test_descent_move_sequence_plain_workload(lg, inst, oracle_mod, seed, mode):
     """n=1000 integer coordinates in [0,1e4)^2, random start: the whole move
-    sequence, the final tour and its length equal the oracle's."""
+    sequence, the final tour and its length equal the oracle's, with the
+    graph-driven and the cooperative persistent descent."""
     xy = inst.uniform_int(1000, seed)
     r = inst.random_tour(1000, seed)
     want, m, log = oracle_mod.descend(xy, r, log_cap=1 << 20)
     with lg.Solver(xy) as s:
+        s.set_descent_mode(lg.DESCENT_GRAPH if mode == "graph" else lg.DESCENT_COOPERATIVE)
         got, trace, st = s.optimize_trace(r)
     assert st["moves"] == m
     assert np.array_equal(trace, log)
@@ -123,13 +126,15 @@ def test_descent_move_sequence_plain_workload(lg, inst, oracle_mod, seed):
     assert st["sweeps"] == m + 1
 
 
+@pytest.mark.parametrize("mode", ["graph", "cooperative"])
 @pytest.mark.parametrize("n,kicks,kind", [(200, 40, 0), (200, 40, 1), (523, 25, 0),
                                           (523, 25, 1), (1500, 6, 1)])
-def test_ils_matches_oracle(lg, inst, oracle_mod, n, kicks, kind):
+def test_ils_matches_oracle(lg, inst, oracle_mod, n, kicks, kind, mode):
     xy = inst.uniform_f32(n, n, 1.0e4)
     r = inst.random_tour(n, n + 1)
     want, ost = oracle_mod.ils(xy, r, kicks, 1234 + n, kind)
     with lg.Solver(xy) as s:
+        s.set_descent_mode(lg.DESCENT_GRAPH if mode == "graph" else lg.DESCENT_COOPERATIVE)
         got, st = s.ils(r, kicks, 1234 + n, kind)
     assert np.array_equal(got, want)
     assert st["final_length"] == ost["best_length"]
@@ -137,6 +142,48 @@ def test_ils_matches_oracle(lg, inst, oracle_mod, n, kicks, kind):
     assert st["moves"] == ost["moves"]
     assert st["accepted"] == ost["accepted"]
     assert st["kicks"] == kicks
+
+
+@pytest.mark.parametrize("n", [8, 2501, 6144])
+def test_cooperative_descent_sizes(lg, inst, oracle_mod, n):
+    """The cooperative descent at its size limits (smallest tour, the switch
+    to 4-row tiles and 512-thread CTAs, the largest cooperative tour): bounded
+    descents, traces and the resident tour agree with the graph-driven
+    descent, whose moves are checked against the oracle elsewhere."""
+    xy = inst.uniform_f32(n, 30 + n, 1.0e6)
+    r = inst.random_tour(n, 31 + n)
+    res = {}
+    for mode in (lg.DESCENT_GRAPH, lg.DESCENT_COOPERATIVE):
+        with lg.Solver(xy) as s:
+            s.set_descent_mode(mode)
+            assert s.info()["descent_mode"] == mode
+            a, st_a = s.optimize(r, max_moves=7)
+            b, tr, st_b = s.optimize_trace(a, max_moves=40)
+            s.set_route(b)
+            st_c = s.descend_resident(max_moves=0)
+            res[mode] = (a, b, tr, s.get_route(), st_a["moves"], st_b["moves"], st_c["moves"],
+                         st_c["sweeps"], s.length_resident())
+    g, c = res[lg.DESCENT_GRAPH], res[lg.DESCENT_COOPERATIVE]
+    for x, y in zip(g, c):
+        if isinstance(x, np.ndarray):
+            assert np.array_equal(x, y)
+        else:
+            assert x == y
+    assert lg.check_tour(c[3])
+
+
+def test_descent_mode_api(lg, inst):
+    xy = inst.uniform_f32(7000, 3, 1.0e6)
+    with lg.Solver(xy) as s:
+        assert s.info()["cooperative_ctas"] == 0
+        assert s.info()["descent_mode"] == lg.DESCENT_GRAPH
+        with pytest.raises(lg.LogoError):
+            s.set_descent_mode(lg.DESCENT_COOPERATIVE)
+        with pytest.raises(lg.LogoError):
+            s.set_descent_mode(7)
+    with lg.Solver(xy[:1000]) as s:
+        assert s.info()["cooperative_ctas"] > 0
+        assert s.info()["descent_mode"] == lg.DESCENT_COOPERATIVE
 
 
 def test_tour_length_and_resident_api(lg, inst, oracle_mod):

@@ -343,6 +343,16 @@ logo_status logo_read_tsplib(const char *path, logo_xy *coords, uint32_t cap, ui
  * lowest id.  Unlike the reference's kd-tree, duplicate points are kept. */
 logo_status logo_nn_tour(const logo_xy *coords, uint32_t n, uint32_t start, uint32_t *route);
 
+/* Multiple-fragment (greedy edge) start tour (multipleFragment_KD,
+ * src/utils/kdtree_utils.c:56-242, the reference's --init mf): repeatedly the
+ * shortest nint edge from a city to its nearest city of degree < 2 outside
+ * its own fragment, taken in the reference's priority-queue order so that
+ * equal lengths are broken the same way; the path is listed from city 0 as
+ * the reference lists it.  Neighbour searches use a uniform grid, ties to the
+ * lowest id (the reference's kd-tree breaks exact distance ties by traversal
+ * order and mishandles duplicate points). */
+logo_status logo_mf_tour(const logo_xy *coords, uint32_t n, uint32_t *route);
+
 /* Seeded random start tour (routeInit with ROUTE_INIT_SHUFFLE,
  * src/utils/construction.c:129-137, which uses random_shuffle on rand()):
  * Fisher-Yates driven by SplitMix64. */

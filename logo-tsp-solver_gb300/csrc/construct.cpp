@@ -3,6 +3,7 @@
 //
 //   logo_read_tsplib   ≙ readFileCoords       src/utils/tsp_loader.c:49-162
 //   logo_nn_tour       ≙ initRoute_KD_NN      src/utils/kdtree_utils.c:279-301
+//   logo_mf_tour       ≙ multipleFragment_KD  src/utils/kdtree_utils.c:56-242
 //   logo_random_tour   ≙ routeInit(SHUFFLE)   src/utils/construction.c:129-137
 //   logo_check_tour    ≙ checkTour            src/utils/construction.c:152-183
 //
@@ -14,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <queue>
 #include <string>
 #include <vector>
 
@@ -70,8 +72,9 @@ public:
     }
 
     // Nearest live city to (px, py) by double Euclidean distance; ties go to
-    // the lower id.
-    uint32_t nearest(double px, double py) const {
+    // the lower id.  Cities skip_a and skip_b are passed over.
+    uint32_t nearest(double px, double py, uint32_t skip_a = UINT32_MAX,
+                     uint32_t skip_b = UINT32_MAX) const {
         uint32_t cx, cy;
         cell_xy(px, py, cx, cy);
         double best = INFINITY;
@@ -86,11 +89,15 @@ public:
                 if (y == ya || y == yb) {  // full row of the ring
                     for (int64_t x = std::max<int64_t>(xa, 0);
                          x <= std::min<int64_t>(xb, gw_ - 1); ++x)
-                        scan_cell((size_t)y * gw_ + (size_t)x, px, py, best, besti);
+                        scan_cell((size_t)y * gw_ + (size_t)x, px, py, skip_a, skip_b, best,
+                                  besti);
                 } else {  // only the two side cells
-                    if (xa >= 0) scan_cell((size_t)y * gw_ + (size_t)xa, px, py, best, besti);
+                    if (xa >= 0)
+                        scan_cell((size_t)y * gw_ + (size_t)xa, px, py, skip_a, skip_b, best,
+                                  besti);
                     if (xb != xa && xb < (int64_t)gw_)
-                        scan_cell((size_t)y * gw_ + (size_t)xb, px, py, best, besti);
+                        scan_cell((size_t)y * gw_ + (size_t)xb, px, py, skip_a, skip_b, best,
+                                  besti);
                 }
             }
         }
@@ -109,9 +116,11 @@ public:
     }
 
 private:
-    void scan_cell(size_t c, double px, double py, double& best, uint32_t& besti) const {
+    void scan_cell(size_t c, double px, double py, uint32_t skip_a, uint32_t skip_b,
+                   double& best, uint32_t& besti) const {
         for (uint32_t t = 0; t < count_[c]; ++t) {
             const uint32_t id = items_[start_[c] + t];
+            if (id == skip_a || id == skip_b) continue;
             const double dx = px - (double)p_[id].x, dy = py - (double)p_[id].y;
             const double d = std::sqrt(dx * dx + dy * dy);
             if (d < best || (d == best && id < besti)) {
@@ -137,6 +146,97 @@ private:
     std::vector<uint32_t> start_, count_, items_, pos_, cell_;
     uint32_t live_cells_;
 };
+
+// nint(|a - b|) as an int: the per-edge distance in binary32 (this file is
+// compiled without FMA contraction), truncated like the reference's
+// fragment.distance (src/defs.h:201-205, from calculateDistance2D,
+// src/headers.h:127-133).
+int nint_dist(const logo_xy& a, const logo_xy& b) {
+    const float dx = a.x - b.x, dy = a.y - b.y;
+    return (int)(std::sqrt(dx * dx + dy * dy) + 0.5f);
+}
+
+// Greedy-edge ("multiple fragment") start tour, following the steps of
+// multipleFragment_KD (src/utils/kdtree_utils.c:56-242) so that equal
+// distances leave the priority queue in the same order: a max-heap (by
+// std::priority_queue) of (nint distance to the current nearest valid
+// neighbour, city); the top city x joins its neighbour y when y still has
+// degree < 2 and is not the far end of x's own fragment, otherwise x's
+// neighbour is looked up again among the cities of degree < 2 other than x
+// and that far end, and x is pushed back.  Cities of degree 2 leave the
+// search grid.  After n - 1 joins the path is listed from city 0: first the
+// side of the neighbour city 0 was joined to first (reversed), then 0, then
+// the side of its second neighbour.
+struct Fragment {
+    int distance;
+    uint32_t id;
+};
+struct LaterFragment {  // the heap's top is the shortest distance
+    bool operator()(const Fragment& a, const Fragment& b) const {
+        return a.distance > b.distance;
+    }
+};
+
+void mf_tour(const logo_xy* p, uint32_t n, uint32_t* route) {
+    if (n <= 2) {
+        for (uint32_t k = 0; k < n; ++k) route[k] = k;
+        return;
+    }
+    NNGrid grid(p, n);
+    std::vector<uint8_t> degree(n, 0);
+    std::vector<uint32_t> link(n), tail(n);
+    std::vector<int64_t> first(n, -1), second(n, -1);  // neighbours in join order
+    std::priority_queue<Fragment, std::vector<Fragment>, LaterFragment> pq;
+    for (uint32_t i = 0; i < n; ++i) {
+        tail[i] = i;
+        link[i] = grid.nearest(p[i].x, p[i].y, i);
+        pq.push(Fragment{nint_dist(p[i], p[link[i]]), i});
+    }
+    for (uint32_t e = 0; e + 1 < n; ++e) {
+        uint32_t x, y;
+        for (;;) {
+            const Fragment f = pq.top();
+            x = f.id;
+            if (degree[x] == 2) {
+                pq.pop();
+                continue;
+            }
+            y = link[x];
+            if (degree[y] < 2 && y != tail[x]) break;
+            // look x's neighbour up again, without x and its fragment's far end
+            link[x] = grid.nearest(p[x].x, p[x].y, x, degree[x] ? tail[x] : x);
+            pq.pop();
+            pq.push(Fragment{nint_dist(p[x], p[link[x]]), x});
+        }
+        for (const uint32_t v : {x, y}) {
+            const uint32_t w = v == x ? y : x;
+            if (degree[v] == 0)
+                first[v] = w;
+            else
+                second[v] = w;
+            if (++degree[v] == 2) grid.remove(v);
+        }
+        const uint32_t tx = tail[x];
+        tail[tx] = tail[y];
+        tail[tail[y]] = tx;
+    }
+    // list the path from city 0
+    auto walk = [&](int64_t from, int64_t at, std::vector<uint32_t>& out) {
+        while (at >= 0) {
+            out.push_back((uint32_t)at);
+            const int64_t nx = first[at] == from ? second[at] : first[at];
+            from = at;
+            at = nx;
+        }
+    };
+    std::vector<uint32_t> before, after;
+    walk(0, first[0], before);
+    walk(0, second[0], after);
+    uint32_t k = 0;
+    for (auto it = before.rbegin(); it != before.rend(); ++it) route[k++] = *it;
+    route[k++] = 0;
+    for (const uint32_t v : after) route[k++] = v;
+}
 
 bool finite_coords(const logo_xy* c, uint32_t n) {
     for (uint32_t k = 0; k < n; ++k)
@@ -164,6 +264,13 @@ logo_status logo_nn_tour(const logo_xy* coords, uint32_t n, uint32_t start, uint
         px = coords[id].x;
         py = coords[id].y;
     }
+    return LOGO_OK;
+}
+
+logo_status logo_mf_tour(const logo_xy* coords, uint32_t n, uint32_t* route) {
+    if (!coords || !route || n == 0 || n > LOGO_MAX_CITIES) return LOGO_ERR_INVALID_ARG;
+    if (!finite_coords(coords, n)) return LOGO_ERR_INVALID_ARG;
+    mf_tour(coords, n, route);
     return LOGO_OK;
 }
 

@@ -43,7 +43,7 @@ EXPORTS = [
     "logo_ctx_get_info", "logo_ctx_set_shape", "logo_ctx_stream", "logo_version",
     "logo_descend_trace", "logo_diag_sqrt_error", "logo_begin_descent",
     "logo_enqueue_sweep", "logo_enqueue_apply", "logo_get_progress",
-    "logo_read_tsplib", "logo_nn_tour", "logo_random_tour", "logo_check_tour",
+    "logo_read_tsplib", "logo_nn_tour", "logo_mf_tour", "logo_random_tour", "logo_check_tour",
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
     "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
     "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
@@ -181,6 +181,7 @@ def load(path=LIB_PATH):
     L.logo_get_progress.argtypes = [_vp, _u64p, ctypes.POINTER(ctypes.c_int)]
     L.logo_read_tsplib.argtypes = [c.c_char_p, _vp, c.c_uint32, _u32p]
     L.logo_nn_tour.argtypes = [_vp, c.c_uint32, c.c_uint32, _u32p]
+    L.logo_mf_tour.argtypes = [_vp, c.c_uint32, _u32p]
     L.logo_random_tour.argtypes = [c.c_uint32, c.c_uint64, _u32p]
     L.logo_check_tour.argtypes = [_u32p, c.c_uint32]
     L.logo_batch_create.argtypes = [c.c_int, c.c_uint32, c.c_uint64, c.POINTER(_vp)]
@@ -377,6 +378,14 @@ def nn_tour(coords, start=0):
     xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
     r = np.zeros(len(xy), dtype=np.uint32)
     _check(load().logo_nn_tour(xy.ctypes.data, len(xy), start, r.ctypes.data_as(_u32p)))
+    return r
+
+
+def mf_tour(coords):
+    """Multiple-fragment (greedy edge) start tour (host only)."""
+    xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
+    r = np.zeros(len(xy), dtype=np.uint32)
+    _check(load().logo_mf_tour(xy.ctypes.data, len(xy), r.ctypes.data_as(_u32p)))
     return r
 
 

@@ -94,6 +94,13 @@ def nn_tour(xy):
     return _route(b, 0)[0]
 
 
+def mf_tour(xy):
+    """The reference's multiple-fragment start tour (multipleFragment_KD)."""
+    n = len(np.asarray(xy).reshape(-1)) // 2
+    b = _run("mf", xy, np.arange(n, dtype=np.uint32))
+    return _route(b, 0)[0]
+
+
 def read_tsp(path):
     with tempfile.TemporaryDirectory() as d:
         fout = os.path.join(d, "out.bin")

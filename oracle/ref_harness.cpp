@@ -11,6 +11,7 @@
 //                                    src/solvers/ILSGlobalSolverSequential.cpp:60-100
 //   CPUSolver::optimizeStep (AVX)    src/solvers/cpuSolver.cpp:143-230
 //   constructKDTree/initRoute_KD_NN  src/utils/kdtree_utils.c:29-52,279-301
+//   multipleFragment_KD              src/utils/kdtree_utils.c:56-242
 //   readFileCoords                   src/utils/tsp_loader.c:49-162
 // What this file adds: NintCPUSolver, whose optimizeStep is the loop of
 // CPUSolver::optimizeStep (i ascending, j ascending, strict <, report
@@ -243,6 +244,10 @@ int main(int argc, char **argv) {
     } else if (cmd == "nn") {  // kd-tree nearest-neighbour start tour
         constructKDTree(c.data(), n);
         std::vector<ROUTE_DATA_TYPE> t = initRoute_KD_NN(n, c.data());
+        put_route(out, t);
+    } else if (cmd == "mf") {  // multiple-fragment (greedy edge) start tour
+        constructKDTree(c.data(), n);
+        std::vector<ROUTE_DATA_TYPE> t = multipleFragment_KD(n, c.data());
         put_route(out, t);
     } else {
         fclose(out);

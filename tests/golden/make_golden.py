@@ -3,7 +3,7 @@
 Every expected value here comes from oracle/_ref/ref_harness, which runs the
 reference's unmodified C++ sources (TwoOptLocalSolver::optimize, routeLength,
 ILSGlobalSolver::kick, ILSGlobalSolverSequential::optimize, initRoute_KD_NN,
-readFileCoords) with the per-edge nint optimizeStep -- see oracle/build_ref.sh.
+multipleFragment_KD, readFileCoords) with the per-edge nint optimizeStep -- see oracle/build_ref.sh.
 Instances are regenerated from (generator, n, seed) by instances.py; each
 fixture stores a SHA-256 of the instance and start tour so a drift of the
 generators is caught before any comparison.
@@ -118,6 +118,27 @@ def nn_tours():
     return {"spec": np.array(rows, dtype=np.int64), "hash": np.array(h), "out": np.array(out)}
 
 
+def mf_tours(refdir):
+    """Multiple-fragment start tours (multipleFragment_KD) on seeded instances
+    and TSPLIB files whose neighbour searches have no exact distance ties."""
+    rows, h, out = [], [], []
+    for gen, sizes in (("uniform_f32", (3, 4, 5, 7, 10, 31, 100, 500, 2000, 10000)),
+                       ("clustered", (5, 10, 100, 500, 2000, 10000)),
+                       ("uniform_int", (4, 6, 10, 100, 500, 2000))):
+        for n in sizes:
+            for seed in (1, 2):
+                xy = make_instance(gen, n, seed)
+                rows.append((GENS.index(gen), n, seed))
+                h.append(digest(xy))
+                out.append(digest(ref.mf_tour(xy)))
+    d = {"spec": np.array(rows, dtype=np.int64), "hash": np.array(h), "out": np.array(out)}
+    for name in ("berlin52", "kroA100", "att532"):
+        xy = ref.read_tsp(os.path.join(refdir, "TSPLIB", name + ".tsp"))
+        d[name + "_xy"] = xy
+        d[name + "_mf"] = ref.mf_tour(xy)
+    return d
+
+
 def tsplib(refdir):
     d = {}
     for name in TSPLIB:
@@ -137,9 +158,15 @@ def tsplib(refdir):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None, help="write only this fixture (e.g. mf_tours)")
     a = ap.parse_args()
     if not ref.available():
         ref.build()
+    if a.only == "mf_tours":
+        np.savez_compressed(os.path.join(HERE, "mf_tours.npz"), **mf_tours(a.ref))
+        print("mf_tours.npz written to", HERE)
+        return
+    np.savez_compressed(os.path.join(HERE, "mf_tours.npz"), **mf_tours(a.ref))
     np.savez_compressed(os.path.join(HERE, "steps.npz"), **steps())
     np.savez_compressed(os.path.join(HERE, "descents_n1000.npz"), **descents())
     np.savez_compressed(os.path.join(HERE, "kicks_ils.npz"), **kicks_and_ils())

@@ -52,6 +52,43 @@ def test_nn_tour_tsplib(lg, oracle_mod, name):
         assert d[0] == d[1] and got[k] < want[k]
 
 
+def _instance(inst, gi, n, seed):
+    if GENS[gi] == "uniform_int":
+        return inst.uniform_int(n, seed)
+    if GENS[gi] == "uniform_f32":
+        return inst.uniform_f32(n, seed, 1.0e4)
+    return inst.clustered(n, seed, side=1.0e6, clusters=max(2, n // 50))
+
+
+def test_mf_tour_matches_reference(lg, inst):
+    """Multiple-fragment tours equal the reference's multipleFragment_KD on
+    every fixture (n = 3..10,000; float, clustered and integer coordinates)."""
+    g = np.load(os.path.join(GOLD, "mf_tours.npz"))
+    for (gi, n, seed), h, out in zip(g["spec"], g["hash"], g["out"]):
+        xy = _instance(inst, gi, int(n), int(seed))
+        assert digest(xy) == h
+        assert digest(lg.mf_tour(xy)) == out, (GENS[gi], int(n), int(seed))
+
+
+@pytest.mark.parametrize("name", ["berlin52", "kroA100", "att532"])
+def test_mf_tour_tsplib(lg, name):
+    g = np.load(os.path.join(GOLD, "mf_tours.npz"))
+    assert np.array_equal(lg.mf_tour(g[name + "_xy"]), g[name + "_mf"])
+
+
+def test_mf_tour_edge_cases(lg, inst):
+    assert list(lg.mf_tour(np.zeros((1, 2), np.float32))) == [0]
+    assert list(lg.mf_tour(np.array([[0, 0], [3, 4]], np.float32))) == [0, 1]
+    dup = np.array([[0, 0], [5, 5], [0, 0], [1, 0], [5, 5], [9, 1]], dtype=np.float32)
+    assert lg.check_tour(lg.mf_tour(dup))
+    xy = inst.clustered(30000, 4, side=1.0e6, clusters=60)
+    assert lg.check_tour(lg.mf_tour(xy))
+    bad = inst.uniform_f32(10, 1, 1.0e4)
+    bad[3, 1] = np.nan
+    with pytest.raises(lg.LogoError):
+        lg.mf_tour(bad)
+
+
 def test_nn_tour_keeps_duplicates(lg):
     xy = np.array([[0, 0], [5, 5], [0, 0], [1, 0], [5, 5]], dtype=np.float32)
     t = lg.nn_tour(xy, 0)

@@ -69,3 +69,11 @@ def test_nn_tour(oracle_mod, inst):
     t, ties = oracle_mod.nn_tour(xy)
     assert ties == 0
     assert np.array_equal(ref.nn_tour(xy), t)
+
+
+def test_mf_tour_live(lg, inst):
+    """The library's multiple-fragment tour against the reference's, run now,
+    on fresh seeds (the fixtures hold other seeds)."""
+    for n, seed in ((777, 31), (4000, 32), (15000, 33)):
+        xy = inst.clustered(n, seed, side=1.0e6, clusters=max(2, n // 100))
+        assert np.array_equal(lg.mf_tour(xy), ref.mf_tour(xy)), n

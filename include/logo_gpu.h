@@ -250,6 +250,24 @@ logo_status logo_batch_run(logo_batch *b, const logo_instance *inst, uint32_t co
                            const logo_batch_opts *opts, logo_result *results,
                            double *device_ms);
 
+/* Multi-start ILS (ILSGlobalSolverMT, src/solvers/ILSGlobalSolverMT.cpp:86-195,
+ * with its --comm sharing when share != 0): `replicas` copies of one instance
+ * (3 <= n <= LOGO_BATCH_MAX_N), replica k kicked from seed + k, all solved in
+ * one persistent launch, one CTA per replica.  Without share every replica
+ * equals logo_ils with its seed.  With share, a replica whose descent does not
+ * beat its own best continues from the best tour any replica has published
+ * (the reference's threads do the same with the global best), and it
+ * publishes its own best whenever that beats the group's; publishing never
+ * waits (a replica that finds another one publishing offers again after its
+ * next descent), so shared runs depend on timing.  route: start tour in, the
+ * best replica's tour out; results (optional) receives one entry per replica,
+ * best (optional) the replica returned; b needs max_count >= replicas and
+ * max_cities >= n * replicas. */
+logo_status logo_batch_multistart(logo_batch *b, const logo_xy *coords, uint32_t n,
+                                  uint32_t *route, uint32_t replicas, uint64_t seed, int share,
+                                  const logo_batch_opts *opts, logo_result *results,
+                                  uint32_t *best, double *device_ms);
+
 /* One-shot logo_batch_create + logo_batch_run + logo_batch_destroy. */
 logo_status logo_batch_solve(const logo_instance *inst, uint32_t count,
                              const logo_batch_opts *opts, logo_result *results,

@@ -32,11 +32,93 @@ namespace logo {
 
 namespace {
 
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned int* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Multi-start sharing (ILSGlobalSolverMT.cpp:86-195 with comm = 1): offers
+// this replica's best tour to its group if it beats the group's best.  The
+// lock is only tried, never waited for; a replica that finds it taken offers
+// again after its next descent.
+template <int NT>
+__device__ void publish_best(SharedBest* g, uint32_t* tours, const uint32_t* bestr, uint32_t n,
+                             unsigned long long best_len, unsigned int* flag) {
+    if (threadIdx.x == 0) {
+        unsigned int f = 0;
+        if (best_len < *(volatile unsigned long long*)&g->best_len &&
+            atomicCAS(&g->lock, 0u, 1u) == 0u) {
+            if (best_len < *(volatile unsigned long long*)&g->best_len) {
+                atomicAdd(&g->seq, 1u);  // odd: rewriting
+                __threadfence();
+                f = 1;
+            } else {
+                atomicExch(&g->lock, 0u);
+            }
+        }
+        *flag = f;
+    }
+    __syncthreads();
+    if (*flag) {
+        uint32_t* t = tours + g->off;
+        for (uint32_t k = threadIdx.x; k < n; k += NT) t[k] = bestr[k];
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            *(volatile unsigned long long*)&g->best_len = best_len;
+            __threadfence();
+            atomicAdd(&g->seq, 1u);  // even: consistent
+            atomicExch(&g->lock, 0u);
+        }
+    }
+    __syncthreads();
+}
+
+// Loads the group's best tour into route / Q (coordinates; the caller
+// recomputes edges) when one is published that is no longer than this
+// replica's best; false (route / Q possibly overwritten) when there is none
+// or it changed while being read.
+template <int NT>
+__device__ bool adopt_best(SharedBest* g, const uint32_t* tours, uint32_t* route,
+                           OrderedCity* Q, const float2* xy, uint32_t n,
+                           unsigned long long best_len, unsigned int* flag, unsigned int* s1) {
+    if (threadIdx.x == 0) {
+        const unsigned int q = ld_acquire_u32(&g->seq);
+        const unsigned long long gl = *(volatile unsigned long long*)&g->best_len;
+        *s1 = q;
+        *flag = !(q & 1u) && gl != ~0ull && gl <= best_len;
+    }
+    __syncthreads();
+    if (!*flag) {
+        __syncthreads();
+        return false;
+    }
+    const uint32_t* t = tours + g->off;
+    for (uint32_t k = threadIdx.x; k < n; k += NT) {
+        const uint32_t c = __ldcg(t + k);
+        route[k] = c < n ? c : 0u;
+        const float2 p = xy[route[k]];
+        Q[k].x = p.x;
+        Q[k].y = p.y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *flag = ld_acquire_u32(&g->seq) == *s1;
+    }
+    __syncthreads();
+    const bool ok = *flag;
+    __syncthreads();
+    return ok;
+}
+
 template <int R, int NT, int TC>
 __global__ void __launch_bounds__(NT)
     batch_kernel(BatchArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ CtaShared<NT> S;
+    __shared__ unsigned int share_flag, share_seq;
     OrderedCity* Q = reinterpret_cast<OrderedCity*>(smem_raw);
     uint32_t* route = reinterpret_cast<uint32_t*>(smem_raw + sizeof(OrderedCity) * A.max_n);
     uint32_t* bestr = route + A.max_n;
@@ -97,24 +179,32 @@ __global__ void __launch_bounds__(NT)
                 }
             }
             if (status) break;
-            // accept (strictly shorter) or revert to the best tour
+            // accept (strictly shorter) or go back: to the replica's own best
+            // tour, or in a multi-start group to the group's best
             const unsigned long long len = tour_length<NT>(S, Q, n);
+            SharedBest* grp = I.group != kNoGroup ? A.shared + I.group : nullptr;
             if (len < best_len) {
                 best_len = len;
                 ++accepted;
                 for (uint32_t k = threadIdx.x; k < n; k += NT) bestr[k] = route[k];
+                __syncthreads();
             } else {
-                for (uint32_t k = threadIdx.x; k < n; k += NT) {
-                    const uint32_t c = bestr[k];
-                    route[k] = c;
-                    const float2 p = xy[c];
-                    Q[k].x = p.x;
-                    Q[k].y = p.y;
+                const bool adopted = grp && adopt_best<NT>(grp, A.shared_tours, route, Q, xy, n,
+                                                           best_len, &share_flag, &share_seq);
+                if (!adopted) {
+                    for (uint32_t k = threadIdx.x; k < n; k += NT) {
+                        const uint32_t c = bestr[k];
+                        route[k] = c;
+                        const float2 p = xy[c];
+                        Q[k].x = p.x;
+                        Q[k].y = p.y;
+                    }
                 }
                 __syncthreads();
                 recompute_edges<NT>(Q, n);
             }
             __syncthreads();
+            if (grp) publish_best<NT>(grp, A.shared_tours, bestr, n, best_len, &share_flag);
             if (it == A.kicks) break;
             // kick: every thread draws the same numbers from the same state
             if (A.kick_kind == 1) {
@@ -161,10 +251,12 @@ static cudaError_t launch_batch_t(const BatchArgs& A, int grid, cudaStream_t s,
                                   int* occupancy) {
     const size_t smem = batch_smem_bytes(A.max_n);
     if (occupancy) {
-        // the attribute is set here, outside any stream capture
+        // the attribute is set here, outside any stream capture, and for the
+        // largest instance (it is shared by every batch object in the process)
+        const size_t cap = batch_smem_bytes(kBatchMaxN);
         cudaError_t e = cudaFuncSetAttribute(batch_kernel<R, NT, TC>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                             (int)(cap > 48 * 1024 ? cap : 48 * 1024));
         if (e != cudaSuccess) return e;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occupancy, batch_kernel<R, NT, TC>,
                                                              NT, smem);

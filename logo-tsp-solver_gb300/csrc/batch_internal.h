@@ -8,11 +8,26 @@ namespace logo {
 
 constexpr uint32_t kBatchMaxN = 4096;  // largest instance a CTA holds in smem
 
+constexpr uint32_t kNoGroup = 0xFFFFFFFFu;
+
 struct BatchInstance {
     unsigned long long off;   // first city of this instance in coords / routes
     unsigned long long seed;  // kick PRNG state
     uint32_t n;
     float margin;             // filter margin for this instance's coordinates
+    uint32_t group;           // shared-best group (multi-start), or kNoGroup
+    uint32_t pad;
+};
+
+// Best tour shared by the replicas of one multi-start group.  A writer holds
+// `lock` (taken with atomicCAS, never waited for) and makes `seq` odd while
+// it rewrites the tour; a reader keeps a copy only if `seq` was even and
+// unchanged around it.
+struct SharedBest {
+    unsigned long long best_len;  // ~0 until the first publication
+    unsigned int lock;
+    unsigned int seq;
+    unsigned long long off;       // the tour's first entry in BatchArgs::shared_tours
 };
 
 struct BatchResult {
@@ -37,6 +52,8 @@ struct BatchArgs {
     uint32_t max_n;           // sizes the dynamic shared memory
     uint32_t kicks;
     int kick_kind;
+    SharedBest* shared;       // per group (null when no instance has a group)
+    uint32_t* shared_tours;   // the groups' best tours
 };
 
 struct BatchShape {

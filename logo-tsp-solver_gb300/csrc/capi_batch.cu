@@ -51,6 +51,8 @@ struct logo_batch {
     BatchInstance* h_inst = nullptr;
     uint32_t* h_order = nullptr;
     BatchResult* h_res = nullptr;
+    SharedBest* d_shared = nullptr;     // multi-start: the group's best (one group)
+    uint32_t* d_shared_tours = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     BatchShape table[kBuckets];
     int sms = 0;
@@ -86,6 +88,8 @@ void free_batch(logo_batch* b) {
     cudaFree(b->d_order);
     cudaFree(b->d_res);
     cudaFree(b->d_queue);
+    cudaFree(b->d_shared);
+    cudaFree(b->d_shared_tours);
     if (b->h_coords) cudaFreeHost(b->h_coords);
     if (b->h_routes) cudaFreeHost(b->h_routes);
     if (b->h_inst) cudaFreeHost(b->h_inst);
@@ -148,6 +152,8 @@ logo_status pack(logo_batch* b, const logo_instance* in, uint32_t count) {
         d.seed = I.seed;
         d.n = I.n;
         d.margin = filter_margin(diag);
+        d.group = kNoGroup;
+        d.pad = 0;
         b->h_inst[k] = d;
         off += I.n;
     }
@@ -188,8 +194,11 @@ std::vector<Group> plan(logo_batch* b, const logo_instance* in, uint32_t count,
     return g;
 }
 
+// share: every instance is a replica of one multi-start group (same n) that
+// shares its best tour.
 logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
-                const logo_batch_opts& o, logo_result* res, double* ms_out) {
+                const logo_batch_opts& o, logo_result* res, double* ms_out,
+                bool share = false) {
     BCK(b, cudaSetDevice(b->device));
     if (o.kick_kind != LOGO_KICK_SEGMENT && o.kick_kind != LOGO_KICK_DOUBLE_BRIDGE)
         return bfail(b, LOGO_ERR_INVALID_ARG, "unknown kick kind");
@@ -205,6 +214,15 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
     }
     std::vector<Group> groups = plan(b, in, count, o);
     const uint64_t cities = b->h_inst[count - 1].off + b->h_inst[count - 1].n;
+    if (share) {
+        if (!b->d_shared) BCK(b, cudaMalloc(&b->d_shared, sizeof(SharedBest)));
+        if (!b->d_shared_tours)
+            BCK(b, cudaMalloc(&b->d_shared_tours, sizeof(uint32_t) * kBatchMaxN));
+        const SharedBest init{~0ull, 0u, 0u, 0ull};
+        BCK(b, cudaMemcpyAsync(b->d_shared, &init, sizeof(init), cudaMemcpyHostToDevice,
+                               b->stream));
+        for (uint32_t k = 0; k < count; ++k) b->h_inst[k].group = 0;
+    }
     BCK(b, cudaMemcpyAsync(b->d_coords, b->h_coords, sizeof(float2) * cities,
                            cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaMemcpyAsync(b->d_routes, b->h_routes, sizeof(uint32_t) * cities,
@@ -242,6 +260,8 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
         A.max_n = groups[gi].max_n;
         A.kicks = o.kicks;
         A.kick_kind = o.kick_kind;
+        A.shared = share ? b->d_shared : nullptr;
+        A.shared_tours = share ? b->d_shared_tours : nullptr;
         ce = launch_batch(A, groups[gi].shape, grids[gi], b->stream, nullptr);
     }
     cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);
@@ -419,6 +439,36 @@ logo_status logo_batch_solve(const logo_instance* inst, uint32_t count,
     if (s != LOGO_OK) g_batch_err = b->err;
     free_batch(b);
     return s;
+}
+
+logo_status logo_batch_multistart(logo_batch* b, const logo_xy* coords, uint32_t n,
+                                  uint32_t* route, uint32_t replicas, uint64_t seed, int share,
+                                  const logo_batch_opts* opts, logo_result* results,
+                                  uint32_t* best, double* device_ms) {
+    if (!b || !opts || !coords || !route) return LOGO_ERR_INVALID_ARG;
+    if (replicas == 0 || replicas > b->max_count)
+        return bfail(b, LOGO_ERR_INVALID_ARG, "replicas outside [1, max_count]");
+    if ((uint64_t)n * replicas > b->max_cities)
+        return bfail(b, LOGO_ERR_INVALID_ARG, "n x replicas exceeds max_cities");
+    std::vector<uint32_t> tours((size_t)n * replicas);
+    std::vector<logo_instance> inst(replicas);
+    for (uint32_t k = 0; k < replicas; ++k) {
+        std::memcpy(tours.data() + (size_t)k * n, route, sizeof(uint32_t) * n);
+        inst[k].coords = coords;
+        inst[k].route = tours.data() + (size_t)k * n;
+        inst[k].n = n;
+        inst[k].seed = seed + k;
+    }
+    std::vector<logo_result> res(replicas);
+    const logo_status s = run(b, inst.data(), replicas, *opts, res.data(), device_ms, share != 0);
+    if (results) std::copy(res.begin(), res.end(), results);
+    if (s != LOGO_OK) return s;
+    uint32_t w = 0;
+    for (uint32_t k = 1; k < replicas; ++k)
+        if (res[k].best_length < res[w].best_length) w = k;
+    std::memcpy(route, tours.data() + (size_t)w * n, sizeof(uint32_t) * n);
+    if (best) *best = w;
+    return LOGO_OK;
 }
 
 logo_status logo_batch_shape_for(const logo_batch* b, uint32_t n, logo_batch_shape* out) {

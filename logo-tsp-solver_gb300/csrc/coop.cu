@@ -32,6 +32,7 @@ namespace logo {
 namespace {
 
 constexpr unsigned long long kCoopWaitNs = 2000000000ull;
+constexpr uint32_t kCoopSmallN = 2500;  // 256-thread CTAs up to here, 512 above
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned int* p) {
     unsigned v;
@@ -232,11 +233,13 @@ size_t coop_smem(uint32_t n) {
 // Grid for a cooperative launch: every CTA resident at once (occupancy x
 // SMs), and no more CTAs than the sweep has warp tiles for.
 template <int R, int TC, int NT>
-int coop_grid_t(uint32_t n, int device) {
+int coop_grid_t(uint32_t n, uint32_t max_n, int device) {
     const size_t smem = coop_smem<R, TC>(n);
+    // the limit is shared by every context: set it for the largest n this
+    // instantiation runs, not for this context's n
     if (cudaFuncSetAttribute(coop_descent_kernel<R, TC, NT>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)coop_smem<R, TC>(max_n)) != cudaSuccess)
         return 0;
     int per_sm = 0, sms = 0, coop = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_descent_kernel<R, TC, NT>,
@@ -271,12 +274,13 @@ cudaError_t launch_coop_t(const CoopArgs& A, int grid, cudaStream_t s) {
 // descent is as fast or faster, so the limit is 6,144).
 int coop_grid(uint32_t n, int device) {
     if (n < 8 || n > kCoopMaxN) return 0;
-    return n <= 2500 ? coop_grid_t<2, 32, 256>(n, device) : coop_grid_t<2, 32, 512>(n, device);
+    return n <= kCoopSmallN ? coop_grid_t<2, 32, 256>(n, kCoopSmallN, device)
+                            : coop_grid_t<2, 32, 512>(n, kCoopMaxN, device);
 }
 
 cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s) {
-    return A.n <= 2500 ? launch_coop_t<2, 32, 256>(A, grid, s)
-                       : launch_coop_t<2, 32, 512>(A, grid, s);
+    return A.n <= kCoopSmallN ? launch_coop_t<2, 32, 256>(A, grid, s)
+                              : launch_coop_t<2, 32, 512>(A, grid, s);
 }
 
 }  // namespace logo

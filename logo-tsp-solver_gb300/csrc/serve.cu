@@ -19,6 +19,7 @@
 
 #include "cta_tour.cuh"
 #include "logo_device.cuh"
+#include "batch_internal.h"
 #include "serve_internal.h"
 #include "sweep_core.cuh"
 
@@ -162,8 +163,10 @@ cudaError_t launch_serve_round(const ServeArgs& A, int grid, cudaStream_t s, int
     const size_t smem = serve_smem_bytes(A.max_n);
     auto kern = serve_round_kernel<kServeR, kServeNT, kServeTC>;
     if (occupancy) {
+        // for the largest request: the attribute is shared by every server
+        const size_t cap = serve_smem_bytes(kBatchMaxN);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                             (int)(cap > 48 * 1024 ? cap : 48 * 1024));
         if (e != cudaSuccess) return e;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occupancy, kern, kServeNT, smem);
     }

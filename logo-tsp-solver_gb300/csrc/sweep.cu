@@ -450,13 +450,20 @@ size_t sweep2_smem_bytes(uint32_t cb) {
     return sweep2_cols_offset(cb) + (size_t)(cb + 1) * sizeof(ColRec);
 }
 
+// The dynamic shared-memory limit is a property of the kernel, shared by
+// every context in the process: it is always set for the largest tile a
+// context may choose (4096 columns), never for this context's own tile, so
+// that contexts created later cannot lower it under another one's launch.
+constexpr uint32_t kMaxTileCols = 4096;
+inline int attr_bytes(size_t smem) { return (int)(smem > 48 * 1024 ? smem : 48 * 1024); }
+
 template <int R, int NW>
 static cudaError_t launch_sweep2_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     const size_t smem = sweep2_smem_bytes(L.cb);
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel2<R, NW>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                    attr_bytes(sweep2_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel2<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
                                                          L.margin, L.st);
@@ -473,7 +480,7 @@ static cudaError_t launch_sweep4_t(const SweepLaunch& L, cudaStream_t s, bool pr
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel4<R, NW>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                    attr_bytes(sweep4_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel4<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb, L.st);
     return cudaGetLastError();
@@ -489,7 +496,7 @@ static cudaError_t launch_sweep5_g(const SweepLaunch& L, cudaStream_t s, bool pr
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel5<R, NW, G>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                    attr_bytes(sweep5_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel5<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
                                                            L.st);
@@ -520,7 +527,7 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel6<R, NW, G>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                    attr_bytes(sweep6_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel6<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
                                                            L.st);
@@ -544,7 +551,7 @@ static cudaError_t launch_sweep3_t(const SweepLaunch& L, cudaStream_t s, bool pr
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel3<R, NW>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                    attr_bytes(sweep_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel3<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb, L.st);
     return cudaGetLastError();
@@ -557,7 +564,7 @@ static cudaError_t launch_sweep_t(const SweepLaunch& L, cudaStream_t s, bool pre
         // opt-in above 48 KB; called once per shape, outside stream capture
         return cudaFuncSetAttribute(sweep_kernel<R, NW>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+                                    attr_bytes(sweep_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles,
                                                         L.cb, L.margin, L.st);

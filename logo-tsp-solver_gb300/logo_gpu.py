@@ -45,7 +45,7 @@ EXPORTS = [
     "logo_enqueue_sweep", "logo_enqueue_apply", "logo_get_progress",
     "logo_read_tsplib", "logo_nn_tour", "logo_mf_tour", "logo_random_tour", "logo_check_tour",
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
-    "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for",
+    "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for", "logo_batch_multistart",
     "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
     "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
     "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
@@ -195,6 +195,9 @@ def load(path=LIB_PATH):
     L.logo_batch_autotune.argtypes = [_vp, _vp, c.c_uint32, c.c_uint32, c.c_int, c.c_char_p,
                                       c.c_int]
     L.logo_batch_shape_for.argtypes = [_vp, c.c_uint32, c.POINTER(BatchShape)]
+    L.logo_batch_multistart.argtypes = [_vp, _vp, c.c_uint32, _u32p, c.c_uint32, c.c_uint64,
+                                        c.c_int, c.POINTER(BatchOpts), _vp,
+                                        c.POINTER(c.c_uint32), c.POINTER(c.c_double)]
     L.logo_best_move_noalloc.argtypes = [_vp, _vp, c.c_uint32, _vp, _vp, _vp]
     L.logo_server_create.argtypes = [c.POINTER(ServerOpts), c.POINTER(_vp)]
     L.logo_server_submit.argtypes = [_vp, _vp, c.c_uint32, _u32p, c.c_uint64, _u64p]
@@ -470,6 +473,26 @@ class Batch:
                                            ctypes.byref(ms)), self._h)
         out = [{k: getattr(r, k) for k, _ in Result._fields_ if k != "pad"} for r in res]
         return rs, out, ms.value
+
+    def multistart(self, coords, route, replicas, seed, share=True, kicks=0,
+                   kind=KICK_SEGMENT):
+        """Multi-start ILS of one instance: returns (best route, per-replica
+        results, index of the replica returned, device_ms)."""
+        xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
+        r = np.array(route, dtype=np.uint32, copy=True)
+        o = BatchOpts()
+        o.device = self.device
+        o.kicks = kicks
+        o.kick_kind = kind
+        res = (Result * replicas)()
+        best = ctypes.c_uint32()
+        ms = ctypes.c_double()
+        _batch_check(load().logo_batch_multistart(
+            self._h, xy.ctypes.data, len(xy), r.ctypes.data_as(_u32p), replicas,
+            int(seed) & ((1 << 64) - 1), int(bool(share)), ctypes.byref(o), res,
+            ctypes.byref(best), ctypes.byref(ms)), self._h)
+        out = [{k: getattr(x, k) for k, _ in Result._fields_ if k != "pad"} for x in res]
+        return r, out, best.value, ms.value
 
     def autotune(self, coords_list, routes, seeds, kicks=0, kind=KICK_SEGMENT,
                  cache_path=None, reuse=False):

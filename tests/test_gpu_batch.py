@@ -92,3 +92,55 @@ def test_batch_rejects_bad_input(lg, inst):
             b.solve([xy], [bad], [1])
         with pytest.raises(lg.LogoError):
             b.solve([xy] * 5, [np.arange(50)] * 5, [1] * 5)
+
+
+def test_multistart_independent_replicas_equal_ils(lg, inst):
+    """Without sharing, replica k of a multi-start run is exactly logo_ils
+    with seed + k, and the tour returned is the best replica's."""
+    n, kicks, seed = 300, 30, 77
+    xy = inst.uniform_f32(n, 3, 1.0e4)
+    r = inst.random_tour(n, 4)
+    with lg.Batch(8, 8 * n) as b:
+        best_r, res, w, _ = b.multistart(xy, r, 6, seed, share=False, kicks=kicks)
+    want = []
+    with lg.Solver(xy) as s:
+        for k in range(6):
+            t, st = s.ils(r, kicks, seed + k, lg.KICK_SEGMENT)
+            want.append((t, st))
+    assert [x["best_length"] for x in res] == [st["final_length"] for _, st in want]
+    assert [x["accepted"] for x in res] == [st["accepted"] for _, st in want]
+    assert w == int(np.argmin([x["best_length"] for x in res]))
+    assert np.array_equal(best_r, want[w][0])
+
+
+def test_multistart_shared_single_replica_equals_ils(lg, inst):
+    """A shared group of one replica publishes and adopts only its own best
+    tour, which is what plain ILS reverts to."""
+    n, kicks, seed = 500, 40, 5
+    xy = inst.clustered(n, 6, side=1.0e6, clusters=5)
+    r = inst.random_tour(n, 7)
+    with lg.Batch(1, n) as b:
+        got, res, w, _ = b.multistart(xy, r, 1, seed, share=True, kicks=kicks,
+                                      kind=lg.KICK_DOUBLE_BRIDGE)
+    with lg.Solver(xy) as s:
+        want, st = s.ils(r, kicks, seed, lg.KICK_DOUBLE_BRIDGE)
+    assert w == 0 and np.array_equal(got, want)
+    assert res[0]["best_length"] == st["final_length"]
+    assert res[0]["accepted"] == st["accepted"]
+
+
+def test_multistart_shared_group(lg, inst, oracle_mod):
+    """64 replicas sharing their best tour: every replica finishes, the tour
+    returned is valid and as long as the best replica reports, and every
+    replica's best is no worse than its start."""
+    n, kicks, seed = 1000, 60, 11
+    xy = inst.uniform_f32(n, 8, 1.0e4)
+    r = inst.random_tour(n, 9)
+    with lg.Batch(64, 64 * n) as b:
+        got, res, w, ms = b.multistart(xy, r, 64, seed, share=True, kicks=kicks)
+        again, res2, _, _ = b.multistart(xy, r, 64, seed, share=True, kicks=kicks)
+    assert all(x["status"] == 0 and x["kicks"] == kicks for x in res + res2)
+    assert lg.check_tour(got) and lg.check_tour(again)
+    assert oracle_mod.tour_length(xy, got) == min(x["best_length"] for x in res)
+    assert all(x["best_length"] <= x["start_length"] for x in res)
+    assert ms > 0

@@ -172,6 +172,25 @@ def test_cooperative_descent_sizes(lg, inst, oracle_mod, n):
     assert lg.check_tour(c[3])
 
 
+def test_contexts_with_different_shared_memory_coexist(lg, inst, oracle_mod):
+    """A kernel's shared-memory limit is one setting for the whole process: a
+    context created later with a smaller tour or tile must not break the
+    launches of one created earlier with a larger one."""
+    big = inst.uniform_f32(6000, 41, 1.0e6)
+    small = inst.uniform_f32(3000, 42, 1.0e6)
+    rb, rs = inst.random_tour(6000, 43), inst.random_tour(3000, 44)
+    with lg.Solver(big) as a:
+        a.set_kernel(lg.SWEEP_LOCAL, 4, 4, 4096)
+        with lg.Solver(small) as b:
+            b.set_kernel(lg.SWEEP_LOCAL, 4, 4, 64)
+            assert a.optimize_step(rb) == oracle_mod.best_move(big, rb)
+            assert b.optimize_step(rs) == oracle_mod.best_move(small, rs)
+            ta, sa = a.optimize(rb, max_moves=50)
+            tb, sb = b.optimize(rs, max_moves=50)
+            assert sa["moves"] == 50 and sb["moves"] == 50
+            assert lg.check_tour(ta) and lg.check_tour(tb)
+
+
 def test_descent_mode_api(lg, inst):
     xy = inst.uniform_f32(7000, 3, 1.0e6)
     with lg.Solver(xy) as s:

@@ -103,9 +103,12 @@ def cmd_sweep(a):
         with lg.Solver(xy) as s:
             s.set_route(r)
             move = s.sweep_resident()
-            ts = _time_sweeps(s, 3 if n >= 1000000 else 12)
-            best = min(ts[1:])
             info = s.info()
+            if a.reps == 0:  # one sweep per size (for profiling): no timing
+                out.append({"n": n, "variant": info["variant"], "move": list(move)})
+                continue
+            ts = _time_sweeps(s, a.reps or (3 if n >= 1000000 else 12))
+            best = min(ts[1:]) if len(ts) > 1 else ts[0]
         ps = pairs(n) / (best / 1e3)
         out.append({"n": n, "pairs": pairs(n), "sweep_ms": best, "pair_evals_per_s": ps,
                     "alu_frac": ps * OPS_PER_PAIR / peak, "variant": info["variant"],
@@ -295,6 +298,8 @@ def main():
     p.add_argument("--n-lo", type=int, default=100)
     p.add_argument("--n-hi", type=int, default=20000)
     p.add_argument("--sizes", default="10000,100000,1000000")
+    p.add_argument("--reps", type=int, default=None,
+                   help="sweep: timed sweeps per size (0: one untimed sweep, for profiling)")
     p.add_argument("--max-large", type=int, default=0,
                    help="serve: requests above the batch limit in flight (0 = default)")
     p.add_argument("--plain", type=int, default=1, help="serve: also time the plain path")

@@ -361,6 +361,37 @@ logo_status logo_read_tsplib(const char *path, logo_xy *coords, uint32_t cap, ui
  * lowest id.  Unlike the reference's kd-tree, duplicate points are kept. */
 logo_status logo_nn_tour(const logo_xy *coords, uint32_t n, uint32_t start, uint32_t *route);
 
+/* TSPLIB EDGE_WEIGHT_TYPE values reported by logo_tsplib_info.  The engine
+ * computes EUC_2D nint distances, as the reference does for every file it
+ * reads (readFileCoords, src/utils/tsp_loader.c:49-162, only loads the
+ * coordinates); the type lets a caller refuse files meant for another metric. */
+#define LOGO_EWT_EUC_2D 0
+#define LOGO_EWT_CEIL_2D 1
+#define LOGO_EWT_ATT 2
+#define LOGO_EWT_GEO 3
+#define LOGO_EWT_OTHER 4
+/* Header of a TSPLIB file: DIMENSION into *n (optional) and EDGE_WEIGHT_TYPE
+ * into *edge_weight_type (optional; EUC_2D when the header has none).
+ * NOT_FOUND if the file cannot be opened, INVALID_ARG without a valid
+ * DIMENSION.  No counterpart in the reference. */
+logo_status logo_tsplib_info(const char *path, uint32_t *n, int *edge_weight_type);
+
+/* Reads a tour (routeInitFromFile, src/utils/common.c:109-128, which reads
+ * a bare list of 1-based ids): either that list or a TSPLIB .tour file
+ * (NAME/TYPE/DIMENSION header, TOUR_SECTION, ids, -1, EOF).  The ids must be
+ * a permutation of 1..n (and match DIMENSION when given); route receives them
+ * 0-based.  With route = NULL only *n is returned.  NOT_FOUND if the file
+ * cannot be opened, INVALID_ARG if it is malformed or n > cap. */
+logo_status logo_read_tour(const char *path, uint32_t *route, uint32_t cap, uint32_t *n);
+
+/* Writes a tour as 1-based ids (saveRouteToAFile, src/utils/common.c:144-192):
+ * with tsplib_header != 0 as a TSPLIB .tour file (NAME `name`, TYPE TOUR,
+ * DIMENSION, TOUR_SECTION, ids, -1, EOF), else as the reference's bare list
+ * (which its reader accepts).  INVALID_ARG unless route is a permutation of
+ * 0..n-1; NOT_FOUND if the file cannot be written. */
+logo_status logo_write_tour(const char *path, const uint32_t *route, uint32_t n,
+                            const char *name, int tsplib_header);
+
 /* Multiple-fragment (greedy edge) start tour (multipleFragment_KD,
  * src/utils/kdtree_utils.c:56-242, the reference's --init mf): repeatedly the
  * shortest nint edge from a city to its nearest city of degree < 2 outside

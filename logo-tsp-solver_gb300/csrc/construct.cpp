@@ -6,10 +6,14 @@
 //   logo_mf_tour       ≙ multipleFragment_KD  src/utils/kdtree_utils.c:56-242
 //   logo_random_tour   ≙ routeInit(SHUFFLE)   src/utils/construction.c:129-137
 //   logo_check_tour    ≙ checkTour            src/utils/construction.c:152-183
+//   logo_read_tour     ≙ routeInitFromFile    src/utils/common.c:109-128
+//   logo_write_tour    ≙ saveRouteToAFile     src/utils/common.c:144-192
+//   logo_tsplib_info   (no counterpart: the reference reads every file as EUC_2D)
 //
 // Compiled with -ffp-contract=off: the nearest-neighbour search compares
 // double distances and must not change with the host's FMA contraction.
 #include <algorithm>
+#include <cctype>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -244,6 +248,21 @@ bool finite_coords(const logo_xy* c, uint32_t n) {
     return true;
 }
 
+// TSPLIB header keyword of a line ("DIMENSION : 52" -> "DIMENSION"), without
+// blanks; `colon` receives the position of ':' or npos.
+std::string header_key(const std::string& s, size_t& colon) {
+    colon = s.find(':');
+    std::string key = s.substr(0, colon == std::string::npos ? s.size() : colon);
+    key.erase(std::remove_if(key.begin(), key.end(), ::isspace), key.end());
+    return key;
+}
+
+std::string header_value(const std::string& s, size_t colon) {
+    std::string v = colon == std::string::npos ? std::string() : s.substr(colon + 1);
+    v.erase(std::remove_if(v.begin(), v.end(), ::isspace), v.end());
+    return v;
+}
+
 }  // namespace
 
 extern "C" {
@@ -272,6 +291,109 @@ logo_status logo_mf_tour(const logo_xy* coords, uint32_t n, uint32_t* route) {
     if (!finite_coords(coords, n)) return LOGO_ERR_INVALID_ARG;
     mf_tour(coords, n, route);
     return LOGO_OK;
+}
+
+logo_status logo_tsplib_info(const char* path, uint32_t* n_out, int* edge_weight_type) {
+    if (!path) return LOGO_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return LOGO_ERR_NOT_FOUND;
+    char line[4096];
+    long dim = -1;
+    int ewt = LOGO_EWT_EUC_2D;  // what the reference assumes for every file
+    while (std::fgets(line, sizeof line, f)) {
+        const std::string s(line);
+        size_t colon;
+        const std::string key = header_key(s, colon);
+        if (key == "NODE_COORD_SECTION" || key == "EOF") break;
+        if (key == "DIMENSION" && colon != std::string::npos)
+            dim = std::strtol(s.c_str() + colon + 1, nullptr, 10);
+        if (key == "EDGE_WEIGHT_TYPE") {
+            const std::string v = header_value(s, colon);
+            ewt = v == "EUC_2D" ? LOGO_EWT_EUC_2D
+                  : v == "CEIL_2D" ? LOGO_EWT_CEIL_2D
+                  : v == "ATT" ? LOGO_EWT_ATT
+                  : v == "GEO" ? LOGO_EWT_GEO
+                  : LOGO_EWT_OTHER;
+        }
+    }
+    std::fclose(f);
+    if (dim <= 0 || (uint64_t)dim > LOGO_MAX_CITIES) return LOGO_ERR_INVALID_ARG;
+    if (n_out) *n_out = (uint32_t)dim;
+    if (edge_weight_type) *edge_weight_type = ewt;
+    return LOGO_OK;
+}
+
+logo_status logo_read_tour(const char* path, uint32_t* route, uint32_t cap, uint32_t* n_out) {
+    if (!path || !n_out) return LOGO_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return LOGO_ERR_NOT_FOUND;
+    // TSPLIB .tour (header, TOUR_SECTION, ids, -1, EOF) or the reference's
+    // bare list of ids; both 1-based
+    std::vector<uint32_t> ids;
+    long dim = -1;
+    bool section = false, bad = false;
+    char line[4096];
+    while (std::fgets(line, sizeof line, f)) {
+        const std::string s(line);
+        size_t colon;
+        const std::string key = header_key(s, colon);
+        if (key.empty()) continue;
+        if (key == "EOF" || key == "-1") break;
+        if (!section && !std::isdigit((unsigned char)key[0])) {
+            if (key == "TOUR_SECTION") section = true;
+            if (key == "DIMENSION" && colon != std::string::npos)
+                dim = std::strtol(s.c_str() + colon + 1, nullptr, 10);
+            continue;
+        }
+        section = true;
+        const char* p = line;
+        char* end;
+        for (;;) {
+            const long v = std::strtol(p, &end, 10);
+            if (end == p) break;
+            if (v == -1) goto done;
+            if (v < 1 || (uint64_t)v > LOGO_MAX_CITIES) {
+                bad = true;
+                goto done;
+            }
+            ids.push_back((uint32_t)(v - 1));
+            p = end;
+        }
+    }
+done:
+    std::fclose(f);
+    if (bad || ids.empty() || (dim > 0 && (long)ids.size() != dim)) return LOGO_ERR_INVALID_ARG;
+    const uint32_t n = (uint32_t)ids.size();
+    std::vector<uint8_t> seen(n, 0);
+    for (const uint32_t v : ids) {
+        if (v >= n || seen[v]) return LOGO_ERR_INVALID_ARG;
+        seen[v] = 1;
+    }
+    *n_out = n;
+    if (!route) return LOGO_OK;  // size query
+    if (n > cap) return LOGO_ERR_INVALID_ARG;
+    std::memcpy(route, ids.data(), sizeof(uint32_t) * n);
+    return LOGO_OK;
+}
+
+logo_status logo_write_tour(const char* path, const uint32_t* route, uint32_t n,
+                            const char* name, int tsplib_header) {
+    if (!path || !route || n == 0) return LOGO_ERR_INVALID_ARG;
+    std::vector<uint8_t> seen(n, 0);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (route[k] >= n || seen[route[k]]) return LOGO_ERR_INVALID_ARG;
+        seen[route[k]] = 1;
+    }
+    FILE* f = std::fopen(path, "w");
+    if (!f) return LOGO_ERR_NOT_FOUND;
+    bool ok = true;
+    if (tsplib_header)
+        ok = std::fprintf(f, "NAME : %s\nTYPE : TOUR\nDIMENSION : %u\nTOUR_SECTION\n",
+                          name && *name ? name : "tour", n) > 0;
+    for (uint32_t k = 0; ok && k < n; ++k) ok = std::fprintf(f, "%u\n", route[k] + 1) > 0;
+    if (ok && tsplib_header) ok = std::fprintf(f, "-1\nEOF\n") > 0;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? LOGO_OK : LOGO_ERR_NOT_FOUND;
 }
 
 logo_status logo_random_tour(uint32_t n, uint64_t seed, uint32_t* route) {
@@ -311,10 +433,9 @@ logo_status logo_read_tsplib(const char* path, logo_xy* coords, uint32_t cap, ui
     long dim = -1;
     bool in_coords = false;
     while (std::fgets(line, sizeof line, f)) {
-        std::string s(line);
-        const size_t colon = s.find(':');
-        std::string key = s.substr(0, colon == std::string::npos ? s.size() : colon);
-        key.erase(std::remove_if(key.begin(), key.end(), ::isspace), key.end());
+        const std::string s(line);
+        size_t colon;
+        const std::string key = header_key(s, colon);
         if (key == "NODE_COORD_SECTION") {
             in_coords = true;
             break;

@@ -44,6 +44,7 @@ EXPORTS = [
     "logo_descend_trace", "logo_diag_sqrt_error", "logo_begin_descent",
     "logo_enqueue_sweep", "logo_enqueue_apply", "logo_get_progress",
     "logo_read_tsplib", "logo_nn_tour", "logo_mf_tour", "logo_random_tour", "logo_check_tour",
+    "logo_tsplib_info", "logo_read_tour", "logo_write_tour",
     "logo_batch_create", "logo_batch_destroy", "logo_batch_last_error", "logo_batch_run",
     "logo_batch_solve", "logo_batch_autotune", "logo_batch_shape_for", "logo_batch_multistart",
     "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
@@ -182,6 +183,9 @@ def load(path=LIB_PATH):
     L.logo_read_tsplib.argtypes = [c.c_char_p, _vp, c.c_uint32, _u32p]
     L.logo_nn_tour.argtypes = [_vp, c.c_uint32, c.c_uint32, _u32p]
     L.logo_mf_tour.argtypes = [_vp, c.c_uint32, _u32p]
+    L.logo_tsplib_info.argtypes = [c.c_char_p, _u32p, c.POINTER(c.c_int)]
+    L.logo_read_tour.argtypes = [c.c_char_p, _u32p, c.c_uint32, _u32p]
+    L.logo_write_tour.argtypes = [c.c_char_p, _u32p, c.c_uint32, c.c_char_p, c.c_int]
     L.logo_random_tour.argtypes = [c.c_uint32, c.c_uint64, _u32p]
     L.logo_check_tour.argtypes = [_u32p, c.c_uint32]
     L.logo_batch_create.argtypes = [c.c_int, c.c_uint32, c.c_uint64, c.POINTER(_vp)]
@@ -390,6 +394,32 @@ def mf_tour(coords):
     r = np.zeros(len(xy), dtype=np.uint32)
     _check(load().logo_mf_tour(xy.ctypes.data, len(xy), r.ctypes.data_as(_u32p)))
     return r
+
+
+EDGE_WEIGHT_TYPES = {0: "EUC_2D", 1: "CEIL_2D", 2: "ATT", 3: "GEO", 4: "OTHER"}
+
+
+def tsplib_info(path):
+    """(dimension, EDGE_WEIGHT_TYPE name) of a TSPLIB file."""
+    n, t = ctypes.c_uint32(), ctypes.c_int()
+    _check(load().logo_tsplib_info(os.fsencode(path), ctypes.byref(n), ctypes.byref(t)))
+    return n.value, EDGE_WEIGHT_TYPES[t.value]
+
+
+def read_tour(path):
+    """A tour file (TSPLIB .tour or a bare id list, 1-based) as 0-based ids."""
+    n = ctypes.c_uint32()
+    _check(load().logo_read_tour(os.fsencode(path), None, 0, ctypes.byref(n)))
+    r = np.zeros(n.value, dtype=np.uint32)
+    _check(load().logo_read_tour(os.fsencode(path), r.ctypes.data_as(_u32p), n.value,
+                                 ctypes.byref(n)))
+    return r
+
+
+def write_tour(path, route, name="tour", tsplib_header=True):
+    r = np.ascontiguousarray(route, dtype=np.uint32)
+    _check(load().logo_write_tour(os.fsencode(path), r.ctypes.data_as(_u32p), len(r),
+                                  name.encode(), int(bool(tsplib_header))))
 
 
 def random_tour(n, seed):

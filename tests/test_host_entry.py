@@ -151,3 +151,53 @@ def test_read_tsplib_fixture_coordinates(lg, tmp_path):
                  "".join(f"{k + 1} {float(x)!r} {float(y)!r}\n" for k, (x, y) in
                          enumerate(xy.astype(np.float64))) + "EOF\n")
     assert np.array_equal(lg.read_tsplib(str(p)), xy)
+
+
+def test_tour_files_round_trip(lg, inst, tmp_path):
+    r = inst.random_tour(777, 5)
+    for header in (True, False):
+        p = str(tmp_path / f"t{int(header)}.tour")
+        lg.write_tour(p, r, name="t777", tsplib_header=header)
+        assert np.array_equal(lg.read_tour(p), r)
+    text = open(str(tmp_path / "t1.tour")).read()
+    assert text.startswith("NAME : t777\n") and "TOUR_SECTION\n" in text
+    assert text.endswith("-1\nEOF\n")
+    assert open(str(tmp_path / "t0.tour")).read().split()[:3] == [str(v + 1) for v in r[:3]]
+
+
+def test_read_tour_formats_and_errors(lg, tmp_path):
+    p = tmp_path / "a.tour"
+    p.write_text("NAME : a\nCOMMENT : x\nTYPE : TOUR\nDIMENSION : 5\nTOUR_SECTION\n"
+                 "3 1\n5\n 2 4 -1\nEOF\n")
+    assert list(lg.read_tour(str(p))) == [2, 0, 4, 1, 3]
+    p.write_text("2\n1\n3\n")  # the reference's bare list
+    assert list(lg.read_tour(str(p))) == [1, 0, 2]
+    for bad in ("DIMENSION : 4\nTOUR_SECTION\n1 2 3\n-1\n",  # too short
+                "TOUR_SECTION\n1 2 2\n-1\n",                  # repeated id
+                "TOUR_SECTION\n1 0 2\n-1\n",                  # 0 is not an id
+                "TOUR_SECTION\n1 4 2\n-1\n",                  # gap in the ids
+                "TOUR_SECTION\n-1\n"):
+        p.write_text(bad)
+        with pytest.raises(lg.LogoError):
+            lg.read_tour(str(p))
+    with pytest.raises(lg.LogoError):
+        lg.read_tour(str(tmp_path / "missing.tour"))
+    with pytest.raises(lg.LogoError):
+        lg.write_tour(str(tmp_path / "w.tour"), np.array([0, 0, 1]))
+
+
+def test_tsplib_info(lg, tmp_path):
+    p = tmp_path / "c.tsp"
+    p.write_text("NAME : c\nTYPE : TSP\nDIMENSION : 3\nEDGE_WEIGHT_TYPE : CEIL_2D\n"
+                 "NODE_COORD_SECTION\n1 0 0\n2 3 4\n3 6 8\nEOF\n")
+    assert lg.tsplib_info(str(p)) == (3, "CEIL_2D")
+    p.write_text("NAME : d\nDIMENSION: 3\nNODE_COORD_SECTION\n1 0 0\n2 3 4\n3 6 8\n")
+    assert lg.tsplib_info(str(p)) == (3, "EUC_2D")
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TSPLIB), reason="reference TSPLIB files absent")
+@pytest.mark.parametrize("name,ewt", [("berlin52", "EUC_2D"), ("att532", "ATT"),
+                                      ("pla7397", "CEIL_2D")])
+def test_tsplib_info_reference_files(lg, name, ewt):
+    n, t = lg.tsplib_info(os.path.join(REF_TSPLIB, name + ".tsp"))
+    assert t == ewt and n == int(name.lstrip("abcdefghijklmnopqrstuvwxyz"))

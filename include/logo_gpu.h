@@ -212,12 +212,19 @@ typedef struct logo_batch_shape {
     int tile_cols;
 } logo_batch_shape;
 
+/* Start tours of a batch: the routes passed in, or nearest-neighbour tours
+ * built on the device (equal to logo_nn_tour from city 0; the routes are then
+ * outputs only). */
+#define LOGO_START_GIVEN 0
+#define LOGO_START_NN 1
+
 typedef struct logo_batch_opts {
     int device;
     uint32_t kicks;         /* ILS kicks per instance; 0 = descent only */
     int kick_kind;          /* LOGO_KICK_* */
     logo_batch_shape shape; /* all zero = use the tuned (or default) table */
     uint32_t ctas;          /* persistent CTAs; 0 = SMs x occupancy */
+    int start;              /* LOGO_START_* */
 } logo_batch_opts;
 
 typedef struct logo_result {

@@ -4,6 +4,7 @@
   python logo-tsp-solver_gb300/bench_suite.py sweep    # one sweep at n=10k, 100k, 1M
   python logo-tsp-solver_gb300/bench_suite.py large    # n=100k NN descent + 1000 kicks
   python logo-tsp-solver_gb300/bench_suite.py serve    # Poisson request stream
+  python logo-tsp-solver_gb300/bench_suite.py construct  # start tours, host vs device
 
 All inputs are seeded synthetic instances (instances.py).  The oracle (CPU
 restatement of the reference) is used only where a line reports a CPU
@@ -138,6 +139,39 @@ def cmd_large(a):
                       "moves": st["moves"], "sweeps": st["sweeps"], "accepted": st["accepted"],
                       "start_length": st["start_length"], "final_length": st["final_length"],
                       "valid_tour": lg.check_tour(tour)}))
+
+
+def cmd_construct(a):
+    """Start tours for the batched workload (4096 instances, n log-uniform in
+    [50, 2000], uniform fp32 in [0,1e4)^2): nearest-neighbour tours built on
+    the host (logo_nn_tour, one instance after another) and then solved, vs
+    built by the batched launch itself (start=START_NN); both then descend to
+    a local optimum.  Also the multiple-fragment tours' host time."""
+    coords, _, seeds = instances.batched_workload(a.count, a.seed, 50, 2000, 1.0e4)
+    total = sum(len(c) for c in coords)
+    t0 = time.perf_counter()
+    nn = [lg.nn_tour(c, 0) for c in coords]
+    host_nn_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mf = [lg.mf_tour(c) for c in coords]
+    host_mf_s = time.perf_counter() - t0
+    with lg.Batch(len(coords), total) as b:
+        b.solve(coords[:64], nn[:64], seeds[:64])  # warm-up
+        t0 = time.perf_counter()
+        r_given, res_given, ms_given = b.solve(coords, nn, seeds)
+        given_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r_dev, res_dev, ms_dev = b.solve(coords, None, seeds, start=lg.START_NN)
+        dev_s = time.perf_counter() - t0
+    same = all(np.array_equal(x, y) for x, y in zip(r_given, r_dev))
+    print(json.dumps({"workload": f"construct: {a.count} instances, n log-uniform [50,2000], "
+                                  "NN start tours, descent to a local optimum",
+                      "host_nn_s": host_nn_s, "host_mf_s": host_mf_s,
+                      "solve_given_nn_device_ms": ms_given, "solve_given_nn_wall_s": given_s,
+                      "solve_device_nn_device_ms": ms_dev, "solve_device_nn_wall_s": dev_s,
+                      "device_construction_ms": ms_dev - ms_given,
+                      "end_to_end_host_nn_s": host_nn_s + given_s,
+                      "end_to_end_device_nn_s": dev_s, "identical_results": same}))
 
 
 def _pool(count, seed, n_lo, n_hi):
@@ -287,8 +321,9 @@ def cmd_serve(a):
 
 def main():
     p = argparse.ArgumentParser()
-    p.add_argument("cmd", choices=["plain", "sweep", "large", "serve"])
+    p.add_argument("cmd", choices=["plain", "sweep", "large", "serve", "construct"])
     p.add_argument("--seeds", type=int, default=4)
+    p.add_argument("--count", type=int, default=4096, help="construct: instances")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--kicks", type=int, default=None)
     p.add_argument("--rates", default="2000,40")
@@ -309,7 +344,8 @@ def main():
     if a.kicks is None:
         a.kicks = {"large": 1000, "serve": 50}.get(a.cmd, 0)
     lg.load()
-    {"plain": cmd_plain, "sweep": cmd_sweep, "large": cmd_large, "serve": cmd_serve}[a.cmd](a)
+    {"plain": cmd_plain, "sweep": cmd_sweep, "large": cmd_large, "serve": cmd_serve,
+     "construct": cmd_construct}[a.cmd](a)
 
 
 if __name__ == "__main__":

@@ -113,6 +113,84 @@ __device__ bool adopt_best(SharedBest* g, const uint32_t* tours, uint32_t* route
     return ok;
 }
 
+// Nearest-neighbour start tour of one instance, built by the CTA (the host
+// logo_nn_tour, itself initRoute_KD_NN of src/utils/kdtree_utils.c:279-301):
+// from city 0's point, repeatedly the nearest unvisited city by the double
+// distance sqrt(dx*dx + dy*dy) (no contraction, as the host computes it), ties
+// to the lowest id.  Each step screens the unvisited cities with the binary32
+// squared distance, whose relative error is below 2.5e-7, so every city whose
+// double distance can be the minimum has a float value within a factor
+// 1 + 1e-6 of the float minimum; only those are evaluated in double.
+template <int NT>
+__device__ void nn_tour_cta(const float2* xy, uint32_t n, uint32_t* route, uint32_t* visited) {
+    __shared__ float red_f[NT / 32];
+    __shared__ double red_d[NT / 32];
+    __shared__ uint32_t red_i[NT / 32];
+    __shared__ uint32_t pick;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t k = threadIdx.x; k < n; k += NT) visited[k] = 0;
+    __syncthreads();
+    float px = xy[0].x, py = xy[0].y;
+    for (uint32_t step = 0; step < n; ++step) {
+        float m = INFINITY;
+        for (uint32_t j = threadIdx.x; j < n; j += NT) {
+            if (visited[j]) continue;
+            const float dx = __fsub_rn(px, xy[j].x), dy = __fsub_rn(py, xy[j].y);
+            m = fminf(m, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        }
+        for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) red_f[warp] = m;
+        __syncthreads();
+        m = red_f[0];
+#pragma unroll
+        for (int w = 1; w < NT / 32; ++w) m = fminf(m, red_f[w]);
+        const float thr = m * (1.0f + 1e-6f) + 1e-30f;
+        double bd = INFINITY;
+        uint32_t bi = 0xFFFFFFFFu;
+        for (uint32_t j = threadIdx.x; j < n; j += NT) {
+            if (visited[j]) continue;
+            const float2 q = xy[j];
+            const float dx = __fsub_rn(px, q.x), dy = __fsub_rn(py, q.y);
+            if (__fmaf_rn(dy, dy, __fmul_rn(dx, dx)) > thr) continue;
+            const double ex = __dsub_rn((double)px, (double)q.x);
+            const double ey = __dsub_rn((double)py, (double)q.y);
+            const double d = __dsqrt_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)));
+            if (d < bd || (d == bd && j < bi)) {
+                bd = d;
+                bi = j;
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+            const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (od < bd || (od == bd && oi < bi)) {
+                bd = od;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            red_d[warp] = bd;
+            red_i[warp] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double d = red_d[0];
+            uint32_t i = red_i[0];
+            for (int w = 1; w < NT / 32; ++w)
+                if (red_d[w] < d || (red_d[w] == d && red_i[w] < i)) {
+                    d = red_d[w];
+                    i = red_i[w];
+                }
+            pick = i < n ? i : 0u;
+            route[step] = pick;
+            visited[pick] = 1;
+        }
+        __syncthreads();
+        px = xy[pick].x;
+        py = xy[pick].y;
+    }
+}
+
 template <int R, int NT, int TC>
 __global__ void __launch_bounds__(NT)
     batch_kernel(BatchArgs A) {
@@ -135,9 +213,10 @@ __global__ void __launch_bounds__(NT)
         const float2* xy = A.coords + I.off;
         uint32_t* rio = A.routes + I.off;
 
-        // load the start tour, its ordered coordinates and edge lengths
+        // load (or build) the start tour, its ordered coordinates and edge lengths
+        if (A.start_nn) nn_tour_cta<NT>(xy, n, route, bestr);
         for (uint32_t k = threadIdx.x; k < n; k += NT) {
-            const uint32_t c = rio[k];
+            const uint32_t c = A.start_nn ? route[k] : rio[k];
             const float2 p = xy[c];
             route[k] = c;
             bestr[k] = c;

@@ -54,6 +54,7 @@ struct BatchArgs {
     int kick_kind;
     SharedBest* shared;       // per group (null when no instance has a group)
     uint32_t* shared_tours;   // the groups' best tours
+    int start_nn;             // build nearest-neighbour start tours instead of loading them
 };
 
 struct BatchShape {

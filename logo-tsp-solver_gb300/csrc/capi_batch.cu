@@ -109,8 +109,9 @@ bool shape_compiled(const BatchShape& s) {
     return false;
 }
 
-// Validates and packs the instances into the pinned staging buffers.
-logo_status pack(logo_batch* b, const logo_instance* in, uint32_t count) {
+// Validates and packs the instances into the pinned staging buffers (the
+// routes only when they are start tours, given = true).
+logo_status pack(logo_batch* b, const logo_instance* in, uint32_t count, bool given = true) {
     if (!in && count) return bfail(b, LOGO_ERR_INVALID_ARG, "instances is NULL");
     if (count > b->max_count) return bfail(b, LOGO_ERR_INVALID_ARG, "count exceeds max_count");
     uint64_t off = 0;
@@ -138,14 +139,18 @@ logo_status pack(logo_batch* b, const logo_instance* in, uint32_t count) {
         if (!(diag < LOGO_MAX_DIAGONAL))
             return bfail(b, LOGO_ERR_INVALID_ARG,
                          "instance " + std::to_string(k) + ": diagonal exceeds LOGO_MAX_DIAGONAL");
-        seen.assign(I.n, 0);
-        for (uint32_t c = 0; c < I.n; ++c) {
-            const uint32_t v = I.route[c];
-            if (v >= I.n || seen[v])
-                return bfail(b, LOGO_ERR_INVALID_ARG,
-                             "instance " + std::to_string(k) + ": route is not a permutation");
-            seen[v] = 1;
-            b->h_routes[off + c] = v;
+        if (given) {
+            seen.assign(I.n, 0);
+            for (uint32_t c = 0; c < I.n; ++c) {
+                const uint32_t v = I.route[c];
+                if (v >= I.n || seen[v])
+                    return bfail(b, LOGO_ERR_INVALID_ARG,
+                                 "instance " + std::to_string(k) + ": route is not a permutation");
+                seen[v] = 1;
+                b->h_routes[off + c] = v;
+            }
+        } else {
+            std::memset(b->h_routes + off, 0, sizeof(uint32_t) * I.n);
         }
         BatchInstance d;
         d.off = off;
@@ -206,7 +211,9 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
     if (fixed && !shape_compiled(BatchShape{o.shape.rows_per_thread, o.shape.threads_per_cta,
                                             o.shape.tile_cols}))
         return bfail(b, LOGO_ERR_INVALID_ARG, "shape is not compiled");
-    logo_status s = pack(b, in, count);
+    if (o.start != LOGO_START_GIVEN && o.start != LOGO_START_NN)
+        return bfail(b, LOGO_ERR_INVALID_ARG, "unknown start-tour kind");
+    logo_status s = pack(b, in, count, o.start == LOGO_START_GIVEN);
     if (s != LOGO_OK) return s;
     if (count == 0) {
         if (ms_out) *ms_out = 0;
@@ -262,6 +269,7 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
         A.kick_kind = o.kick_kind;
         A.shared = share ? b->d_shared : nullptr;
         A.shared_tours = share ? b->d_shared_tours : nullptr;
+        A.start_nn = o.start == LOGO_START_NN;
         ce = launch_batch(A, groups[gi].shape, grids[gi], b->stream, nullptr);
     }
     cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);

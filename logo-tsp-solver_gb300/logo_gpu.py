@@ -30,6 +30,8 @@ SWEEP_LOCAL = 5
 DESCENT_AUTO = 0
 DESCENT_GRAPH = 1
 DESCENT_COOPERATIVE = 2
+START_GIVEN = 0
+START_NN = 1
 MAX_CITIES = 2097152
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",
@@ -96,7 +98,8 @@ class BatchShape(ctypes.Structure):
 
 class BatchOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("kicks", ctypes.c_uint32),
-                ("kick_kind", ctypes.c_int), ("shape", BatchShape), ("ctas", ctypes.c_uint32)]
+                ("kick_kind", ctypes.c_int), ("shape", BatchShape), ("ctas", ctypes.c_uint32),
+                ("start", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -487,13 +490,18 @@ class Batch:
             arr[k].seed = int(seeds[k]) & ((1 << 64) - 1)
         return arr, xs, rs
 
-    def solve(self, coords_list, routes, seeds, kicks=0, kind=KICK_SEGMENT, shape=None, ctas=0):
-        """Returns (routes, results as a list of dicts, device_ms)."""
+    def solve(self, coords_list, routes, seeds, kicks=0, kind=KICK_SEGMENT, shape=None, ctas=0,
+              start=START_GIVEN):
+        """Returns (routes, results as a list of dicts, device_ms).  With
+        start=START_NN the routes are built on the device (routes may be None)."""
+        if routes is None:
+            routes = [np.zeros(len(np.asarray(c).reshape(-1, 2)), np.uint32) for c in coords_list]
         arr, xs, rs = self._pack(coords_list, routes, seeds)
         o = BatchOpts()
         o.device = self.device
         o.kicks = kicks
         o.kick_kind = kind
+        o.start = start
         if shape:
             o.shape = BatchShape(*shape)
         o.ctas = ctas

@@ -144,3 +144,37 @@ def test_multistart_shared_group(lg, inst, oracle_mod):
     assert oracle_mod.tour_length(xy, got) == min(x["best_length"] for x in res)
     assert all(x["best_length"] <= x["start_length"] for x in res)
     assert ms > 0
+
+
+@pytest.mark.parametrize("kicks", [0, 5])
+def test_batch_nn_start_built_on_device(lg, inst, kicks):
+    """start=START_NN: each CTA builds the nearest-neighbour tour of its
+    instance; results equal the single-instance path started from the host
+    logo_nn_tour (integer coordinates included: exact distance ties and
+    duplicate points)."""
+    coords, seeds = [], []
+    for k, n in enumerate([50, 97, 300, 1000, 2000, 3000, 4096]):
+        s = 700 + k
+        if k % 3 == 0:
+            xy = inst.uniform_int(n, s)
+            xy = np.floor(xy / 50.0).astype(np.float32)  # many ties and duplicates
+        elif k % 3 == 1:
+            xy = inst.uniform_f32(n, s, 1.0e4)
+        else:
+            xy = inst.clustered(n, s, side=1.0e6, clusters=max(2, n // 200))
+        coords.append(xy)
+        seeds.append(s)
+    total = sum(len(c) for c in coords)
+    with lg.Batch(len(coords), total) as b:
+        got, res, _ = b.solve(coords, None, seeds, kicks=kicks, start=lg.START_NN)
+    for xy, g, r, s in zip(coords, got, res, seeds):
+        nn = lg.nn_tour(xy, 0)
+        with lg.Solver(xy) as sol:
+            if kicks:
+                want, st = sol.ils(nn, kicks, s, lg.KICK_SEGMENT)
+                assert r["best_length"] == st["final_length"]
+            else:
+                want, st = sol.optimize(nn)
+                assert r["best_length"] == st["final_length"]
+            assert r["start_length"] == st["start_length"]
+        assert np.array_equal(g, want), len(xy)

@@ -494,6 +494,15 @@ void *logo_ctx_stream(logo_ctx *ctx);
 /* Library version string. */
 const char *logo_version(void);
 
+/* Test hook for failure detection (no counterpart in the reference): runs
+ * two device waits that nothing will satisfy -- an mbarrier expecting bytes
+ * that no copy delivers (the sweeps' staging wait) and the cooperative
+ * descent's grid barrier with one of two CTAs missing -- and returns the
+ * status bits each left (1 = gave up after its 2 s budget) and the time the
+ * pair took.  Nothing faults or hangs; the device stays usable. */
+logo_status logo_diag_wait_limits(int device, uint32_t *mbarrier_status,
+                                  uint32_t *barrier_status, double *waited_ms);
+
 /* Self-check of the sweep's exactness argument: the largest relative error of
  * the device's approximate square root over every positive normal binary32
  * input, against the correctly rounded root.  The sweep's filter margin

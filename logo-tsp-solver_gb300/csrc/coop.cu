@@ -264,7 +264,20 @@ cudaError_t launch_coop_t(const CoopArgs& A, int grid, cudaStream_t s) {
                                        dim3(NT), args, coop_smem<R, TC>(A.n), s);
 }
 
+// Test hook for the bounded wait: one CTA waits at a barrier sized for two,
+// which nothing else will reach; the wait gives up after its budget and sets
+// kErrTimeout in st->status.
+__global__ void barrier_probe_kernel(CoopSync* cs, DevState* st) {
+    __shared__ bool ok;
+    grid_barrier(cs, 2u, st, &ok);
+}
+
 }  // namespace
+
+cudaError_t launch_barrier_probe(CoopSync* cs, DevState* st, cudaStream_t s) {
+    barrier_probe_kernel<<<1, 32, 0, s>>>(cs, st);
+    return cudaGetLastError();
+}
 
 // Warp tiles of 64 rows x 32 columns; 256-thread CTAs up to 2,500 cities,
 // 512 above (measured on GB300, random tours, microseconds per move: n = 1000

@@ -1,9 +1,13 @@
 // Diagnostics: exhaustive error measurement of the approximate square root
-// that the sweep's filter relies on (logo_diag_sqrt_error).
+// that the sweep's filter relies on (logo_diag_sqrt_error), and a check that
+// the device-side waits give up (logo_diag_wait_limits).
 #include <cstring>
+
+#include <chrono>
 
 #include "../../include/logo_gpu.h"
 #include "logo_device.cuh"
+#include "logo_internal.h"
 
 namespace {
 
@@ -32,7 +36,63 @@ __global__ void sqrt_error_kernel(uint32_t lo, uint32_t hi,
     if ((threadIdx.x & 31) == 0) atomicMax(max_bits, w);
 }
 
+// An mbarrier that is told to expect 16 bytes which no copy will deliver:
+// the bounded wait of the sweep kernels gives up after its budget and sets
+// kErrTimeout.  No copy is in flight when the CTA exits.
+__global__ void mbar_probe_kernel(unsigned int* status) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        logo::mbar_init(&bar, 1);
+        logo::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) logo::mbar_arrive_expect_tx(&bar, 16);
+    __syncthreads();
+    logo::mbar_wait_bounded(&bar, 0, status);
+}
+
 }  // namespace
+
+extern "C" logo_status logo_diag_wait_limits(int device, uint32_t* mbarrier_status,
+                                             uint32_t* barrier_status, double* waited_ms) {
+    if (!mbarrier_status || !barrier_status) return LOGO_ERR_INVALID_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return LOGO_ERR_NO_DEVICE;
+    unsigned int* d_status = nullptr;
+    logo::CoopSync* cs = nullptr;
+    logo::DevState* st = nullptr;
+    logo_status rc = LOGO_OK;
+    if (cudaMalloc(&d_status, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc(&cs, sizeof(logo::CoopSync)) != cudaSuccess ||
+        cudaMalloc(&st, sizeof(logo::DevState)) != cudaSuccess) {
+        rc = LOGO_ERR_OOM;
+    } else {
+        cudaMemset(d_status, 0, sizeof(unsigned int));
+        cudaMemset(cs, 0, sizeof(logo::CoopSync));
+        cudaMemset(st, 0, sizeof(logo::DevState));
+        const auto t0 = std::chrono::steady_clock::now();
+        mbar_probe_kernel<<<1, 32>>>(d_status);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = logo::launch_barrier_probe(cs, st, nullptr);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        const auto t1 = std::chrono::steady_clock::now();
+        unsigned int a = 0, b = 0;
+        if (e == cudaSuccess) e = cudaMemcpy(&a, d_status, sizeof(a), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(&b, &st->status, sizeof(b), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            rc = LOGO_ERR_CUDA;
+        } else {
+            *mbarrier_status = a;
+            *barrier_status = b;
+            if (waited_ms)
+                *waited_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        }
+    }
+    cudaFree(d_status);
+    cudaFree(cs);
+    cudaFree(st);
+    return rc;
+}
 
 extern "C" logo_status logo_diag_sqrt_error(int device, double* max_rel_err) {
     if (!max_rel_err) return LOGO_ERR_INVALID_ARG;

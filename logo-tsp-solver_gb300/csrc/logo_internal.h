@@ -59,6 +59,8 @@ struct CoopArgs {
 // CTAs for a cooperative launch at this n on `device` (0: not available).
 int coop_grid(uint32_t n, int device);
 cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s);
+// One CTA waits at the cooperative grid barrier sized for two (test hook).
+cudaError_t launch_barrier_probe(CoopSync* cs, DevState* st, cudaStream_t s);
 
 // Builds Q[0] from xy and route[0] (route already uploaded to route[0]) and
 // checks that route[0] is a permutation of 0..n-1 (st->bad_route = 1 if not;

@@ -43,7 +43,7 @@ EXPORTS = [
     "logo_descend", "logo_ils", "logo_tour_length", "logo_set_route", "logo_get_route",
     "logo_descend_resident", "logo_sweep_resident", "logo_length_resident", "logo_sync",
     "logo_ctx_get_info", "logo_ctx_set_shape", "logo_ctx_stream", "logo_version",
-    "logo_descend_trace", "logo_diag_sqrt_error", "logo_begin_descent",
+    "logo_descend_trace", "logo_diag_sqrt_error", "logo_diag_wait_limits", "logo_begin_descent",
     "logo_enqueue_sweep", "logo_enqueue_apply", "logo_get_progress",
     "logo_read_tsplib", "logo_nn_tour", "logo_mf_tour", "logo_random_tour", "logo_check_tour",
     "logo_tsplib_info", "logo_read_tour", "logo_write_tour",
@@ -179,6 +179,9 @@ def load(path=LIB_PATH):
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
                                      c.c_uint64, c.POINTER(Stats)]
     L.logo_diag_sqrt_error.argtypes = [c.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.logo_diag_wait_limits.argtypes = [c.c_int, ctypes.POINTER(ctypes.c_uint32),
+                                        ctypes.POINTER(ctypes.c_uint32),
+                                        ctypes.POINTER(ctypes.c_double)]
     L.logo_begin_descent.argtypes = [_vp, c.c_uint64]
     L.logo_enqueue_sweep.argtypes = [_vp]
     L.logo_enqueue_apply.argtypes = [_vp]
@@ -442,6 +445,17 @@ def sqrt_error(device=0):
     v = ctypes.c_double()
     _check(load().logo_diag_sqrt_error(device, ctypes.byref(v)))
     return v.value
+
+
+def wait_limits(device=0):
+    """Runs two device waits that nothing satisfies (an mbarrier expecting
+    bytes no copy delivers, the cooperative grid barrier missing a CTA) and
+    returns (mbarrier_status, barrier_status, waited_ms); each status holds
+    the timeout bit (1) when its wait gave up (see logo_diag_wait_limits)."""
+    a, b, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+    _check(load().logo_diag_wait_limits(device, ctypes.byref(a), ctypes.byref(b),
+                                        ctypes.byref(ms)))
+    return a.value, b.value, ms.value
 
 
 def _batch_check(status, b):

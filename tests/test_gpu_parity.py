@@ -317,6 +317,26 @@ def test_sqrt_error_bound(lg):
     assert 0 < err <= 2.0 ** -23, err
 
 
+def test_device_waits_give_up_then_context_usable(lg, inst, oracle_mod):
+    """Failure detection without a fault: an mbarrier that expects bytes no
+    copy delivers, and the cooperative grid barrier with one of its two CTAs
+    missing, each give up after their 2 s budget and leave the timeout bit;
+    the device then still solves correctly."""
+    mbar, barrier, ms = lg.wait_limits(0)
+    assert mbar == 1 and barrier == 1, (mbar, barrier)
+    assert 3900.0 <= ms <= 30000.0, ms
+    xy = _instance(inst, 300, 5)
+    r = inst.random_tour(300, 105)
+    with lg.Solver(xy) as s:
+        assert s.optimize_step(r) == oracle_mod.best_move(xy, r)
+        got, st = s.optimize(r, max_moves=5)
+    want = r.copy()
+    for _ in range(5):
+        d, i, j = oracle_mod.best_move(xy, want)
+        want = oracle_mod.apply_move(want, i, j)
+    assert np.array_equal(got, want) and st["moves"] == 5
+
+
 GROUPED_KERNELS = [(4, 4, 4, 256), (4, 4, 2, 256), (4, 4, 8, 128), (4, 8, 4, 512), (4, 8, 8, 256),
                    (4, 16, 4, 1024), (5, 4, 4, 256), (5, 4, 2, 256), (5, 4, 8, 128),
                    (5, 8, 4, 512), (5, 8, 8, 256), (5, 16, 4, 1024)]

@@ -166,7 +166,11 @@ SWEEP_KERNELS = {0: ("sweep_kernel", "MUFU screen"),
                  2: ("sweep_kernel3", "square-root-free screen"),
                  3: ("sweep_kernel4", "packed square-root-free screen"),
                  4: ("sweep_kernel5", "fused two-stage square-root-free screen"),
-                 5: ("sweep_kernel6", "local-coordinate expanded screen")}
+                 5: ("sweep_kernel6", "local-coordinate expanded screen"),
+                 6: ("sweep_boxed_kernel", "boxed screen: row-block and window bounding "
+                                           "boxes, then the local-coordinate screen")}
+# kernels per sweep launch: the boxed variant runs window_stats_kernel and tile_filter_kernel first
+SWEEP_LAUNCHES = {6: 3}
 
 
 def profile_traffic(kernel):
@@ -287,8 +291,10 @@ def run_ours(a, world, rank, local, dist):
         "unit": "TFLOP/s",
         "frac": round(achieved_pairs * OPS_PER_PAIR / peak_ops, 4),
         "traffic": profile_traffic(kname),
-        "kernel": f"logo::{kname}<{info['rows_per_thread']},{info['warps_per_cta']}> "
-                  f"({screen}, {info['tile_cols']}-column tiles)",
+        "kernel": ("logo::window_stats_kernel + logo::tile_filter_kernel + "
+                   if SWEEP_LAUNCHES.get(info["variant"]) else "")
+                  + f"logo::{kname}<{info['rows_per_thread']},{info['warps_per_cta']}> "
+                  f"({screen}, {info['tile_cols']}-column tiles; timed together)",
         "ops_per_pair": "6 FP32 + 4 INT (algorithmic convention, 1 distance/pair)",
         "peak_source": f"152 SMs x 128 FP32/INT32 lanes x sm_max_mhz={sm_max:g} "
                        "(MEASURED_PEAKS.json)",
@@ -305,7 +311,8 @@ def run_ours(a, world, rank, local, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded Gaussian mixture, no dataset)",
         "config": config(n, world), "roofline": roof, "e2e": e2e, "clocks": clocks,
-        "gpu_launches": 2 * a.steps, "wall_s_timed_region": round(t_wall, 3),
+        "gpu_launches": (SWEEP_LAUNCHES.get(info["variant"], 1) + 1) * a.steps,
+        "wall_s_timed_region": round(t_wall, 3),
     }
 
     if a.batched and rank == 0:

@@ -471,19 +471,28 @@ logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
  * LOGO_SWEEP_LOCAL: the test on d(i, c) expanded in coordinates relative to
  *   the tile's first row, |q|^2 - 2 r.q against a per-row threshold with a
  *   proven rounding margin (two FFMA per pair), then the fused screen's
- *   remaining stages. */
+ *   remaining stages.
+ * LOGO_SWEEP_BOXED: three launches per sweep.  (1) The bounding box and
+ *   largest edge of every 32-city window; (2) a tile filter that keeps only
+ *   tiles with a (32-row window, 32-column window) pair whose box distance
+ *   lets some pair be chosen; (3) a persistent sweep over the kept tiles
+ *   that tests each thread's rows against each window's box with the live
+ *   best delta before running the local screen on what is left.  Tile
+ *   widths must be multiples of 32 up to 1024. */
 #define LOGO_SWEEP_MUFU 0
 #define LOGO_SWEEP_MUFU_PACKED 1
 #define LOGO_SWEEP_SQUARED 2
 #define LOGO_SWEEP_SQUARED_PACKED 3
 #define LOGO_SWEEP_FUSED 4
 #define LOGO_SWEEP_LOCAL 5
+#define LOGO_SWEEP_BOXED 6
 /* Selects variant and tile shape together (logo_ctx_set_shape keeps the
  * variant).  Shapes per variant: SQUARED (R,NW) in {(2,2),(4,2),(4,4),(8,4),
  * (8,8),(16,4)}; MUFU {(2,2),(2,4),(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)};
  * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED
  * {(4,4),(8,4),(8,8),(16,4)}; FUSED {(4,2),(4,4),(4,8),(8,2),(8,4),(8,8),(16,4)};
- * LOCAL {(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096. */
+ * LOCAL and BOXED {(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096
+ * (BOXED: a multiple of 32, at most 1024). */
 logo_status logo_ctx_set_kernel(logo_ctx *ctx, int variant, int rows_per_thread,
                                 int warps_per_cta, uint32_t tile_cols);
 

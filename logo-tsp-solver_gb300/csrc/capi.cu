@@ -35,6 +35,12 @@ struct logo_ctx {
     DevState* h_st = nullptr;  // pinned mirror
     uint32_t* h_route = nullptr;  // pinned staging
     uint32_t* d_seen = nullptr;   // bitmap of the route permutation check
+    float4* d_wbox = nullptr;     // per-window boxes and largest edges (boxed sweep)
+    float* d_wmax = nullptr;
+    float4* d_rbox = nullptr;
+    float* d_rmax = nullptr;
+    uint4* d_work = nullptr;      // boxed sweep: tiles that pass the window test
+    uint32_t* d_workctl = nullptr;
     CoopSync* d_coop = nullptr;   // barrier and best-key slots of the cooperative descent
     int coop_grid = 0;            // CTAs of the cooperative descent (0: unavailable)
     int descent_mode = LOGO_DESCENT_AUTO;
@@ -103,6 +109,12 @@ SweepLaunch sweep_args(const logo_ctx* c) {
     L.variant = c->variant;
     L.margin = c->margin;
     L.st = c->d_st;
+    L.wbox = c->d_wbox;
+    L.wmax = c->d_wmax;
+    L.rbox = c->d_rbox;
+    L.rmax = c->d_rmax;
+    L.work = c->d_work;
+    L.workctl = c->d_workctl;
     return L;
 }
 
@@ -111,25 +123,31 @@ uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) /
 // Default tile shape by size (overridable through logo_ctx_set_shape and
 // logo_ctx_set_kernel).
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
-    // measured on GB300 (one sweep, NN start tours and states 5% into their
-    // descents): from n = 17.5k up the local-coordinate screen is fastest
-    // (n = 100k: 0.633 ms vs 0.834 ms fused, 1.16 ms packed squared, 1.72 ms
-    // MUFU; n = 20k: 0.070 ms with 64-column tiles vs 0.083 MUFU; n = 1M random
-    // tour: 54.6 ms vs 70.9 fused); below it the MUFU screen, whose test is
-    // tighter on short tours, wins, with 64-column tiles from 3k (n = 10k:
-    // 0.030 ms vs 0.042 with (4, 4, 128) tiles; n = 15k: 0.052 vs 0.060 local).
+    // measured on GB300 (one sweep: NN start tours of Gaussian mixtures, the
+    // local optimum of the n = 100k one, uniform points on random tours): from
+    // n = 17.5k up the boxed screen is fastest (n = 100k NN tour: 0.107 ms with
+    // (4, 4, 256) tiles vs 0.61 local, 0.83 fused, 1.80 MUFU; at its local
+    // optimum 0.144 vs 0.68; random tour 0.33 vs 0.68, 0.27 with 512-column
+    // tiles; n = 40k: 0.068 ms with 64-column tiles vs 0.087 with 256 and
+    // 0.149 local; n = 20k: 0.064 vs 0.067 local and 0.084 MUFU; n = 1M random
+    // tour: 8.5 ms with (8, 8, 1024) vs 54.8 local); below it the MUFU screen,
+    // whose test is tighter on short tours, wins, with 64-column tiles from 3k
+    // (n = 10k: 0.030 ms vs 0.059 boxed and 0.042 with (4, 4, 128) MUFU tiles).
     variant = LOGO_SWEEP_MUFU;
-    if (n >= 60000) {
-        variant = LOGO_SWEEP_LOCAL;
+    if (n >= 300000) {
+        variant = LOGO_SWEEP_BOXED;
+        R = 8; NW = 8; cb = 1024;
+    } else if (n >= 200000) {
+        variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 512;
-    } else if (n >= 45000) {
-        variant = LOGO_SWEEP_LOCAL;
+    } else if (n >= 80000) {
+        variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 256;
-    } else if (n >= 30000) {
-        variant = LOGO_SWEEP_LOCAL;
+    } else if (n >= 50000) {
+        variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 128;
     } else if (n >= 17500) {
-        variant = LOGO_SWEEP_LOCAL;
+        variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 64;
     } else if (n >= 3000) {
         R = 4; NW = 2; cb = 64;
@@ -176,9 +194,14 @@ logo_status rebuild(logo_ctx* c) {
         cudaFree(c->d_tiles);
         c->d_tiles = nullptr;
     }
+    if (c->d_work) {
+        cudaFree(c->d_work);
+        c->d_work = nullptr;
+    }
     std::vector<uint2> tiles = make_tiles(c->n, c->R, c->NW, c->cb);
     c->ntiles = (uint32_t)tiles.size();
     if (c->ntiles) {
+        CK(c, cudaMalloc(&c->d_work, sizeof(uint4) * tiles.size()));
         CK(c, cudaMalloc(&c->d_tiles, sizeof(uint2) * tiles.size()));
         CK(c, cudaMemcpy(c->d_tiles, tiles.data(), sizeof(uint2) * tiles.size(),
                          cudaMemcpyHostToDevice));
@@ -373,6 +396,12 @@ void destroy(logo_ctx* c) {
     cudaFree(c->d_st);
     cudaFree(c->d_tiles);
     cudaFree(c->d_seen);
+    cudaFree(c->d_wbox);
+    cudaFree(c->d_wmax);
+    cudaFree(c->d_rbox);
+    cudaFree(c->d_rmax);
+    cudaFree(c->d_work);
+    cudaFree(c->d_workctl);
     cudaFree(c->d_coop);
     if (c->h_st) cudaFreeHost(c->h_st);
     if (c->h_route) cudaFreeHost(c->h_route);
@@ -489,6 +518,11 @@ logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_
     CKC(cudaMallocHost(&c->h_st, sizeof(DevState)));
     CKC(cudaMallocHost(&c->h_route, sizeof(uint32_t) * n));
     CKC(cudaMalloc(&c->d_seen, sizeof(uint32_t) * ((n + 31) / 32)));
+    CKC(cudaMalloc(&c->d_wbox, sizeof(float4) * sweep_windows(n)));
+    CKC(cudaMalloc(&c->d_wmax, sizeof(float) * sweep_windows(n)));
+    CKC(cudaMalloc(&c->d_rbox, sizeof(float4) * sweep_row_windows(n)));
+    CKC(cudaMalloc(&c->d_rmax, sizeof(float) * sweep_row_windows(n)));
+    CKC(cudaMalloc(&c->d_workctl, 2 * sizeof(uint32_t)));
     c->coop_grid = coop_grid(n, device);
     if (c->coop_grid > 0) CKC(cudaMalloc(&c->d_coop, sizeof(CoopSync)));
     std::memset(c->h_st, 0, sizeof(DevState));
@@ -538,7 +572,8 @@ logo_status logo_ctx_set_descent_mode(logo_ctx* c, int mode) {
 
 logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
-    if (!sweep_shape_supported(R, NW, c->variant) || cb < 16 || cb > 4096)
+    if (!sweep_shape_supported(R, NW, c->variant) || cb < 16 || cb > 4096 ||
+        !sweep_cols_supported(c->variant, cb))
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape");
     CK(c, cudaSetDevice(c->device));
     CK(c, cudaStreamSynchronize(c->stream));
@@ -550,9 +585,10 @@ logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
 
 logo_status logo_ctx_set_kernel(logo_ctx* c, int variant, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
-    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_LOCAL)
+    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_BOXED)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown sweep variant");
-    if (!sweep_shape_supported(R, NW, variant) || cb < 16 || cb > 4096)
+    if (!sweep_shape_supported(R, NW, variant) || cb < 16 || cb > 4096 ||
+        !sweep_cols_supported(variant, cb))
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape for this variant");
     CK(c, cudaSetDevice(c->device));
     CK(c, cudaStreamSynchronize(c->stream));

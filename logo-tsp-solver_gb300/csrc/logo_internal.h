@@ -17,10 +17,34 @@ struct SweepLaunch {
     uint32_t ntiles;
     uint32_t cb;         // columns per tile
     int R, NW;           // rows per thread, warps per CTA
-    int variant;         // LOGO_SWEEP_* (0 MUFU, 1 MUFU f32x2, 2 squared, 3 squared f32x2, 4 fused, 5 local)
+    int variant;         // LOGO_SWEEP_* (0 MUFU, 1 MUFU f32x2, 2 squared, 3 squared f32x2, 4 fused, 5 local, 6 boxed)
     float margin;        // filter margin M
     DevState* st;
+    // boxed variant (6): per 32-column window (columns 3 + 32g ..) its coordinate
+    // bounding box and largest edge (sweep_windows(n) entries), the same per
+    // 32-row window (rows 1 + 32g .., sweep_row_windows(n) entries), the list
+    // of (tile, column-window mask) that pass the window test (ntiles entries)
+    // and its two counters (items, items claimed)
+    float4* wbox;
+    float* wmax;
+    float4* rbox;
+    float* rmax;
+    uint4* work;
+    uint32_t* workctl;
 };
+// Windows of the boxed variant: columns 3 + 32 g .. 3 + 32 g + 31 (< n) and
+// rows 1 + 32 g .. 1 + 32 g + 31 (rows with pairs: i + 3 <= n).
+__host__ __device__ inline uint32_t sweep_windows(uint32_t n) {
+    return n < 4 ? 1 : (n - 3 + 31) / 32;
+}
+__host__ __device__ inline uint32_t sweep_row_windows(uint32_t n) {
+    return n < 4 ? 1 : (n - 3 + 31) / 32;
+}
+// The boxed variant needs tile widths that are multiples of 32 (tile column
+// starts are then 3 + 32k) and at most 1024 (one mask bit per window).
+inline bool sweep_cols_supported(int variant, uint32_t cb) {
+    return variant != 6 || (cb % 32 == 0 && cb <= 1024);
+}
 cudaError_t launch_sweep(const SweepLaunch& L, cudaStream_t s);
 // Sets the kernel attributes of L's shape; call before any stream capture.
 cudaError_t launch_sweep_prepare(const SweepLaunch& L);

@@ -309,7 +309,6 @@ __host__ __device__ constexpr size_t sweep6_cx_offset(uint32_t cb) {
 __host__ __device__ constexpr size_t sweep6_wmax_offset(uint32_t cb) {
     return sweep6_cx_offset(cb) + 3 * sweep6_cols4(cb) * sizeof(float);
 }
-
 template <int R, int NW, int G>
 __global__ void __launch_bounds__(NW * 32)
     sweep_kernel6(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
@@ -377,7 +376,253 @@ __global__ void __launch_bounds__(NW * 32)
     __syncthreads();
     if (staged) {
         const ColTile6 t{cx, cy, cc, stage};
-        walk_columns6<R, G>(rb, t, wmax, col0, col0, col_end, ib, n, st, bs);
+        walk_columns6<R, G, false>(rb, t, wmax, nullptr, 0u, col0, col0, col_end, ib, n, st, bs);
+    }
+
+    const uint64_t best = warp_min_u64(bs.best);
+    if (lane == 0 && best != kNoMove) atomicMin(&st->best_key, (unsigned long long)best);
+}
+
+// Boxed variant, pass 1: for every window of 32 columns (columns 3 + 32 g
+// .. 3 + 32 g + 31, below n) the bounding box of its coordinates and its
+// largest edge, and the same for every window of 32 rows (rows 1 + 32 g ..,
+// only rows with pairs, i + 3 <= n; a window without such rows gets an
+// empty box and -3e7), one warp per window.  Also clears the work-list
+// counters of pass 2.
+__device__ __forceinline__ void window_reduce(float& m, float& x0, float& x1, float& y0,
+                                              float& y1) {
+    for (int o = 16; o; o >>= 1) {
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    window_stats_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
+                        uint32_t n, float4* __restrict__ wbox, float* __restrict__ wmax,
+                        float4* __restrict__ rbox, float* __restrict__ rmax,
+                        uint32_t* __restrict__ workctl, DevState* st) {
+    if (*(volatile unsigned int*)&st->converged) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        workctl[0] = 0u;
+        workctl[1] = 0u;
+    }
+    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
+    const uint32_t g = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (g < sweep_windows(n)) {  // whole warps
+        const uint32_t c = 3 + g * kWin6 + lane;
+        const bool in = c < n;
+        const OrderedCity q = Q[in ? c : n - 1];
+        float m = in ? q.e : 0.f;
+        float x0 = in ? q.x : FLT_MAX, x1 = in ? q.x : -FLT_MAX;
+        float y0 = in ? q.y : FLT_MAX, y1 = in ? q.y : -FLT_MAX;
+        window_reduce(m, x0, x1, y0, y1);
+        if (lane == 0) {
+            wbox[g] = make_float4(x0, x1, y0, y1);
+            wmax[g] = m;
+        }
+    }
+    if (g < sweep_row_windows(n)) {
+        const uint32_t i = 1 + g * kWin6 + lane;
+        const bool in = i + 3 <= n;
+        const OrderedCity q = Q[in ? i : 1];
+        float m = in ? q.e : -3.0e7f;
+        float x0 = in ? q.x : FLT_MAX, x1 = in ? q.x : -FLT_MAX;
+        float y0 = in ? q.y : FLT_MAX, y1 = in ? q.y : -FLT_MAX;
+        window_reduce(m, x0, x1, y0, y1);
+        if (lane == 0) {
+            rbox[g] = make_float4(x0, x1, y0, y1);
+            rmax[g] = m;
+        }
+    }
+}
+
+// Boxed variant, pass 2: one warp per tile.  Lane c holds column window c
+// of the tile; for every row window r of the tile it tests whether some
+// pair of (row window r) x (column window c) can be chosen with B = -1, the
+// largest best delta a sweep can end with (box_block6 with the windows'
+// boxes and u = -1 + E_r + 5 + E_c, which bounds every V + 5 of those
+// pairs).  Tiles with a passing pair are appended to the work list as
+// (row0, col0, mask of their column windows that passed).
+__global__ void __launch_bounds__(256)
+    tile_filter_kernel(const uint2* __restrict__ tiles, uint32_t ntiles, uint32_t n,
+                       uint32_t rows_per_tile, uint32_t cb, const float4* __restrict__ wbox,
+                       const float* __restrict__ wmax, const float4* __restrict__ rbox,
+                       const float* __restrict__ rmax, uint4* __restrict__ work,
+                       uint32_t* __restrict__ workctl, DevState* st) {
+    if (*(volatile unsigned int*)&st->converged) return;
+    const uint32_t t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (t >= ntiles) return;  // whole warps
+    const uint2 tile = tiles[t];
+    const uint32_t row0 = tile.x, col0 = tile.y;
+    const uint32_t row_end = min(row0 + rows_per_tile, n - 2);  // rows i + 3 <= n
+    const uint32_t col_end = min(col0 + cb, n);
+    const uint32_t nrw = (row_end - row0 + kWin6 - 1) / kWin6;
+    const uint32_t ncw = (col_end - col0 + kWin6 - 1) / kWin6;  // <= 32
+    const bool has_col = lane < ncw;
+    const uint32_t cw = (col0 - 3) / kWin6 + (has_col ? lane : 0);
+    const float4 cbx = wbox[cw];
+    const float ce = wmax[cw];
+    const uint32_t last_col = min(col0 + (lane + 1) * kWin6, col_end) - 1;
+    const uint32_t rw0 = (row0 - 1) / kWin6;
+    bool any = false;
+    for (uint32_t base = 0; base < nrw; base += 32) {
+        // lane k loads row window base + k; the loop broadcasts them
+        const uint32_t nr = min(32u, nrw - base);
+        const uint32_t rw = rw0 + base + (lane < nr ? lane : 0);
+        const float4 rbl = rbox[rw];
+        const float rel = rmax[rw];
+        for (uint32_t r = 0; r < nr; ++r) {
+            const float4 rb = make_float4(__shfl_sync(0xffffffffu, rbl.x, r),
+                                          __shfl_sync(0xffffffffu, rbl.y, r),
+                                          __shfl_sync(0xffffffffu, rbl.z, r),
+                                          __shfl_sync(0xffffffffu, rbl.w, r));
+            const float re = __shfl_sync(0xffffffffu, rel, r);
+            if (!has_col || last_col < row0 + (base + r) * kWin6 + 2) continue;  // no c >= i + 2
+            const float u = (re + 4.f) + ce;
+            const float gx = fmaxf(fmaxf(__fsub_rn(cbx.x, rb.y), __fsub_rn(rb.x, cbx.y)), 0.f);
+            const float gy = fmaxf(fmaxf(__fsub_rn(cbx.z, rb.w), __fsub_rn(rb.z, cbx.w)), 0.f);
+            const float s = __fmaf_rn(gy, gy, __fmul_rn(gx, gx));
+            any |= u > 0.f && s < __fmul_rn(u, u);
+        }
+    }
+    const uint32_t mask = __ballot_sync(0xffffffffu, any);
+    if (lane == 0 && mask) work[atomicAdd(&workctl[0], 1u)] = make_uint4(row0, col0, mask, 0u);
+}
+
+// Boxed variant, pass 3 (LOGO_SWEEP_BOXED): a persistent grid takes the work
+// list's tiles one at a time.  Per tile: the local-coordinate screen of
+// sweep_kernel6, where each thread first tests the bounding box of its rows
+// against the passing windows' boxes with its current B (box_block6); only
+// the column range of windows some thread can use is staged (one bulk copy)
+// and converted.  Tile columns start at 3 + 32k (tile widths are multiples of
+// 32) and rows at 1 + 32k, so tile window w is window (col0 - 3) / 32 + w of
+// pass 1.  The best delta found carries over from tile to tile and is
+// tightened with the sweep's shared best at every claim (a random tour's
+// large improvements are found by the first tiles; without the refresh a
+// CTA kept the B it started with).  A CTA claims its next item only when it
+// is free (claiming ahead left items
+// reserved by busy CTAs while others ran out: n = 100k local optimum 0.20 ms
+// vs 0.16).
+struct BoxedSlot {
+    uint32_t idx;
+    uint32_t need;            // windows some thread of the CTA may use
+    unsigned long long best;  // the sweep's best key when the item was claimed
+    uint4 item;               // row0, col0, column-window mask
+};
+
+// Resident CTAs per SM the boxed kernel is compiled for (register budget):
+// 4-row, 4-warp CTAs at 96 registers fit 5 per SM (measured faster than 4
+// at 125 registers); the other shapes keep about their unconstrained counts.
+constexpr int boxed_min_blocks(int R, int NW) {
+    return R == 4 ? (NW == 4 ? 5 : NW == 8 ? 2 : 8) : R == 8 ? 2 : 1;
+}
+
+template <int R, int NW, int G>
+__global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
+    sweep_boxed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
+                       uint32_t n, uint32_t cb, const float4* __restrict__ gbox,
+                       const float* __restrict__ gmax, const uint4* __restrict__ work,
+                       uint32_t* __restrict__ workctl, DevState* st) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    BoxedSlot* slot = reinterpret_cast<BoxedSlot*>(smem_raw + 48);  // 32 bytes
+    OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
+    float* cx = reinterpret_cast<float*>(smem_raw + sweep6_cx_offset(cb));
+    float* cy = cx + sweep6_cols4(cb);
+    float* cc = cy + sweep6_cols4(cb);
+
+    if (*(volatile unsigned int*)&st->converged) return;
+    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
+    const uint32_t items = workctl[0];
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Best5 bs;
+    bs.best = kNoMove;
+    bs.B = -1;
+    {
+        const uint64_t gk = *(volatile unsigned long long*)&st->best_key;
+        if (gk != kNoMove) bs.B = min(bs.B, key_delta(gk));
+    }
+    bs.G = bs.B;
+    uint32_t parity = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t idx = atomicAdd(&workctl[1], 1u);
+            slot->idx = idx;
+            slot->need = 0u;
+            slot->best = *(volatile unsigned long long*)&st->best_key;
+            if (idx < items) slot->item = work[idx];
+        }
+        __syncthreads();  // the slot is ready (the previous tile ended in a barrier)
+        if (slot->idx >= items) break;
+        const uint4 item = slot->item;
+        {
+            const uint64_t gk = slot->best;
+            if (gk != kNoMove) {
+                const int g = key_delta(gk);
+                if (g < bs.B) bs.B = g;
+                if (g < bs.G) bs.G = g;
+            }
+        }
+        const uint32_t row0 = item.x, col0 = item.y;
+        const uint32_t col_end = min(col0 + cb, n);
+        const float4* tbox = gbox + (col0 - 3) / kWin6;
+        const float* tmax = gmax + (col0 - 3) / kWin6;
+        const uint32_t ib = row0 + (warp * 32 + lane) * R;
+        bs.busy = false;
+        const OrderedCity origin = Q[row0];  // same for every thread of the tile
+        RowBlock6<R> rb;
+        load_rows6<R>(rb, Q, ib, n, origin.x, origin.y);
+        refresh6<R>(rb, Q, ib, n, bs.B);
+        uint32_t mask = 0;  // windows this thread's rows may use
+        if (ib + 3 <= n) {
+            for (uint32_t m = item.z; m; m &= m - 1) {
+                const uint32_t w = __ffs(m) - 1;
+                if (col0 + (w + 1) * kWin6 <= ib + 2) continue;  // left of the first pair
+                if (box_block6<R>(rb, __ldg(tbox + w), __ldg(tmax + w))) mask |= 1u << w;
+            }
+        }
+        if (mask) atomicOr(&slot->need, mask);
+        __syncthreads();
+        const uint32_t all = slot->need;
+        bool ok = true;
+        if (all) {  // the same for every thread
+            const uint32_t wlo = __ffs(all) - 1, whi = 31 - __clz(all);
+            // stage[k] = column col0 - 1 + k for k in [k0, k1)
+            const uint32_t k0 = wlo * kWin6, k1 = min((whi + 1) * kWin6, col_end - col0) + 1;
+            if (threadIdx.x == 0) {
+                const uint32_t bytes = (k1 - k0) * (uint32_t)sizeof(OrderedCity);
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(bar, bytes);
+                bulk_g2s(stage + k0, Q + (col0 - 1 + k0), bytes, bar);
+            }
+            ok = mbar_wait_bounded(bar, parity, &st->status);
+            parity ^= 1u;
+            if (ok) {
+                for (uint32_t k = k0 + 1 + threadIdx.x; k < k1; k += NW * 32) {
+                    const OrderedCity q = stage[k];
+                    const float p = __fsub_rn(q.x, origin.x), qq = __fsub_rn(q.y, origin.y);
+                    cx[k - 1] = p;
+                    cy[k - 1] = qq;
+                    cc[k - 1] = __fmaf_rn(qq, qq, __fmul_rn(p, p));
+                }
+            }
+            // a copy that did not arrive ends the CTA's work (status has the timeout)
+            if (__syncthreads_or(!ok)) break;
+            if (mask) {
+                const ColTile6 t{cx, cy, cc, stage};
+                walk_columns6<R, G, true>(rb, t, tmax, tbox, mask, col0, col0, col_end, ib, n,
+                                          st, bs);
+            }
+        }
+        __syncthreads();  // every thread has read the slot and the tile's shared memory
     }
 
     const uint64_t best = warp_min_u64(bs.best);
@@ -458,6 +703,7 @@ size_t sweep2_smem_bytes(uint32_t cb) {
 // context may choose (4096 columns), never for this context's own tile, so
 // that contexts created later cannot lower it under another one's launch.
 constexpr uint32_t kMaxTileCols = 4096;
+constexpr uint32_t kMaxBoxedCols = 1024;  // one mask bit per 32-column window
 inline int attr_bytes(size_t smem) { return (int)(smem > 48 * 1024 ? smem : 48 * 1024); }
 
 template <int R, int NW>
@@ -524,8 +770,35 @@ size_t sweep6_smem_bytes(uint32_t cb) {
     return sweep6_wmax_offset(cb) + ((size_t)cb / kWin6 + 2) * sizeof(float);
 }
 
-template <int R, int NW, int G>
+template <int R, int NW, int G, bool BOX>
 static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool prepare) {
+    if (BOX) {
+        // stage and column arrays only; the window statistics stay in global memory
+        const size_t smem = sweep6_wmax_offset(L.cb);
+        if (prepare) {
+            return cudaFuncSetAttribute(sweep_boxed_kernel<R, NW, G>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        attr_bytes(sweep6_wmax_offset(kMaxBoxedCols)));
+        }
+        int device = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&device);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_boxed_kernel<R, NW, G>,
+                                                              NW * 32, smem);
+        if (e != cudaSuccess) return e;
+        const uint32_t resident = (uint32_t)(per_sm > 0 ? per_sm : 1) * (uint32_t)sms;
+        const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
+        const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
+        window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.n, L.wbox, L.wmax,
+                                                           L.rbox, L.rmax, L.workctl, L.st);
+        tile_filter_kernel<<<(L.ntiles + 7) / 8, 256, 0, s>>>(
+            L.tiles, L.ntiles, L.n, (uint32_t)(NW * 32 * R), L.cb, L.wbox, L.wmax, L.rbox,
+            L.rmax, L.work, L.workctl, L.st);
+        sweep_boxed_kernel<R, NW, G><<<grid, NW * 32, smem, s>>>(
+            L.Q0, L.Q1, L.n, L.cb, L.wbox, L.wmax, L.work, L.workctl, L.st);
+        return cudaGetLastError();
+    }
     const size_t smem = sweep6_smem_bytes(L.cb);
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel6<R, NW, G>,
@@ -540,15 +813,15 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
 // Column groups of the local-coordinate screen: 128 / R columns per branch
 // (measured on GB300 with 4-row blocks: n = 100k 0.631 ms with 32 columns vs
 // 0.641 with 16; n = 1M 54.7 ms vs 55.5), 4 below kSweep5GroupMinN cities.
-template <int R, int NW>
+template <int R, int NW, bool BOX>
 static cudaError_t launch_sweep6_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     constexpr int G = (128 / R) < 32 ? (128 / R) : 32;
     if (prepare) {
-        const cudaError_t e = launch_sweep6_g<R, NW, 4>(L, s, true);
-        return e != cudaSuccess ? e : launch_sweep6_g<R, NW, G>(L, s, true);
+        const cudaError_t e = launch_sweep6_g<R, NW, 4, BOX>(L, s, true);
+        return e != cudaSuccess ? e : launch_sweep6_g<R, NW, G, BOX>(L, s, true);
     }
-    return L.n >= kSweep5GroupMinN ? launch_sweep6_g<R, NW, G>(L, s, false)
-                                   : launch_sweep6_g<R, NW, 4>(L, s, false);
+    return L.n >= kSweep5GroupMinN ? launch_sweep6_g<R, NW, G, BOX>(L, s, false)
+                                   : launch_sweep6_g<R, NW, 4, BOX>(L, s, false);
 }
 
 template <int R, int NW>
@@ -578,14 +851,25 @@ static cudaError_t launch_sweep_t(const SweepLaunch& L, cudaStream_t s, bool pre
 }
 
 static cudaError_t dispatch_sweep(const SweepLaunch& L, cudaStream_t s, bool prepare) {
+    if (L.variant == 6) {
+        switch (L.R * 100 + L.NW) {
+            case 402: return launch_sweep6_t<4, 2, true>(L, s, prepare);
+            case 404: return launch_sweep6_t<4, 4, true>(L, s, prepare);
+            case 408: return launch_sweep6_t<4, 8, true>(L, s, prepare);
+            case 804: return launch_sweep6_t<8, 4, true>(L, s, prepare);
+            case 808: return launch_sweep6_t<8, 8, true>(L, s, prepare);
+            case 1604: return launch_sweep6_t<16, 4, true>(L, s, prepare);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     if (L.variant == 5) {
         switch (L.R * 100 + L.NW) {
-            case 402: return launch_sweep6_t<4, 2>(L, s, prepare);
-            case 404: return launch_sweep6_t<4, 4>(L, s, prepare);
-            case 408: return launch_sweep6_t<4, 8>(L, s, prepare);
-            case 804: return launch_sweep6_t<8, 4>(L, s, prepare);
-            case 808: return launch_sweep6_t<8, 8>(L, s, prepare);
-            case 1604: return launch_sweep6_t<16, 4>(L, s, prepare);
+            case 402: return launch_sweep6_t<4, 2, false>(L, s, prepare);
+            case 404: return launch_sweep6_t<4, 4, false>(L, s, prepare);
+            case 408: return launch_sweep6_t<4, 8, false>(L, s, prepare);
+            case 804: return launch_sweep6_t<8, 4, false>(L, s, prepare);
+            case 808: return launch_sweep6_t<8, 8, false>(L, s, prepare);
+            case 1604: return launch_sweep6_t<16, 4, false>(L, s, prepare);
             default: return cudaErrorInvalidValue;
         }
     }
@@ -655,7 +939,7 @@ cudaError_t launch_sweep_prepare(const SweepLaunch& L) {
 }
 
 bool sweep_shape_supported(int R, int NW, int variant) {
-    if (variant == 5) {
+    if (variant == 5 || variant == 6) {
         switch (R * 100 + NW) {
             case 402: case 404: case 408: case 804: case 808: case 1604:
                 return true;

@@ -63,6 +63,8 @@ struct RowBlock6 {
     float T2[R];                 // B + e[ib + r] + 5, or -3e7 for rows without pairs
     float T[R];                  // stage-1 threshold for the current window
     float NL[R];                 // -L of pair row r for the current window (stage 2)
+    float4 rbox;                 // bounding box (x0, x1, y0, y1) of the R pair rows
+    float T2max;                 // max over r of T2[r]
 };
 
 template <int R>
@@ -85,10 +87,17 @@ __device__ __forceinline__ void load_rows6(RowBlock6<R>& rb, const OrderedCity* 
 template <int R>
 __device__ __forceinline__ void refresh6(RowBlock6<R>& rb, const OrderedCity* Q, uint32_t ib,
                                          uint32_t n, int B) {
+    rb.T2max = -3.0e7f;
+    rb.rbox = make_float4(rb.gx[1], rb.gx[1], rb.gy[1], rb.gy[1]);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const uint32_t i = ib + r;
         rb.T2[r] = (i + 3 <= n) ? (float)(B + (int)Q[i].e + 5) : -3.0e7f;
+        rb.T2max = fmaxf(rb.T2max, rb.T2[r]);
+        rb.rbox.x = fminf(rb.rbox.x, rb.gx[r + 1]);
+        rb.rbox.y = fmaxf(rb.rbox.y, rb.gx[r + 1]);
+        rb.rbox.z = fminf(rb.rbox.z, rb.gy[r + 1]);
+        rb.rbox.w = fmaxf(rb.rbox.w, rb.gy[r + 1]);
     }
 }
 
@@ -114,6 +123,7 @@ __device__ __forceinline__ void lower_b6(RowBlock6<R>& rb, int& B, int g) {
     const float shift = (float)(g - B);
 #pragma unroll
     for (int r = 0; r < R; ++r) rb.T2[r] += shift;
+    rb.T2max += shift;
     B = g;
 }
 
@@ -216,12 +226,64 @@ __device__ __forceinline__ bool group6(const RowBlock6<R>& rb, const ColTile6& t
     return pass;
 }
 
+// Window test of the boxed screen (LOGO_SWEEP_BOXED): box = (X0, X1, Y0, Y1),
+// the bounding box of the window's column coordinates (global binary32
+// values).  Rows that cannot be chosen in any column of the window get
+// T = -FLT_MAX; false when no row of the thread is left.
+//
+// Why no chosen pair is missed.  For a column c of the window and row i at
+// (x, y), |x - x_c| >= gx where gx is the real gap between x and [X0, X1]
+// (0 inside), and the gap is one exact binary32 difference (X0 - x or
+// x - X1), so rounding is monotone: |RN(x - x_c)| >= RN(gx).  The reference
+// squares dx = RN(x - x_c), dy = RN(y - y_c); with s = RN(gy^2 + RN(gx^2))
+// (two roundings, each up by at most 2^-24 relative),
+// dx^2 + dy^2 >= s (1 + 2^-24)^-2.  A chosen pair needs
+// dx^2 + dy^2 < (V + 0.5)^2 (1 + 2^-22) (sweep_core5.cuh), so
+// s < (V + 0.5)^2 (1 + 2^-21) <= (V + 5)^2 (1 - 2^-24) <= L for every
+// V < 1.6e7 (here V < 4e6), L = RN(u^2) the row's stage-2 threshold of the
+// window (u >= V + 5).  Rows with u <= 0 have L = 0 and fail s < L.  Lowering
+// B later in the window only tightens the thresholds (window6 recomputes T
+// for every row; the rows this test removed then pass through stage 1 again,
+// which costs work but changes no result).
+// The same test for the thread's rows together, before any per-row work:
+// every row lies in rb.rbox, so the gap between the two boxes (again one
+// exact binary32 difference per axis) bounds every |RN(x - x_c)|, and
+// u = T2max + E bounds every row's u.
+template <int R>
+__device__ __forceinline__ bool box_block6(const RowBlock6<R>& rb, float4 box, float emax) {
+    const float u = rb.T2max + emax;
+    const float gx = fmaxf(fmaxf(__fsub_rn(box.x, rb.rbox.y), __fsub_rn(rb.rbox.x, box.y)), 0.f);
+    const float gy = fmaxf(fmaxf(__fsub_rn(box.z, rb.rbox.w), __fsub_rn(rb.rbox.z, box.w)), 0.f);
+    const float s = __fmaf_rn(gy, gy, __fmul_rn(gx, gx));
+    return u > 0.f && s < __fmul_rn(u, u);
+}
+
+template <int R>
+__device__ __forceinline__ bool box_rows6(RowBlock6<R>& rb, float4 box) {
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const float x = rb.gx[r + 1], y = rb.gy[r + 1];
+        const float gx = fmaxf(fmaxf(__fsub_rn(box.x, x), __fsub_rn(x, box.y)), 0.f);
+        const float gy = fmaxf(fmaxf(__fsub_rn(box.z, y), __fsub_rn(y, box.w)), 0.f);
+        const float s = __fmaf_rn(gy, gy, __fmul_rn(gx, gx));
+        const bool ok = s < -rb.NL[r];
+        rb.T[r] = ok ? rb.T[r] : -FLT_MAX;
+        any |= ok;
+    }
+    return any;
+}
+
 // Walks columns [c_lo, c_hi) of the tile whose first column is col0.
-// wmax[w] = largest e over columns [col0 + w*kWin6, col0 + (w+1)*kWin6).
+// wmax[w] = largest e over columns [col0 + w*kWin6, col0 + (w+1)*kWin6) and,
+// with BOX, wbox[w] = the bounding box of their coordinates (both in global
+// memory) and mask = the windows whose box test passed at the start: the
+// others, and those whose test fails with the current B, are skipped.
 // Sharing of B between threads as in walk_columns5.
-template <int R, int G>
+template <int R, int G, bool BOX>
 __device__ __forceinline__ void walk_columns6(RowBlock6<R>& rb, const ColTile6& t,
-                                              const float* wmax, uint32_t col0, uint32_t c_lo,
+                                              const float* wmax, const float4* wbox,
+                                              uint32_t mask, uint32_t col0, uint32_t c_lo,
                                               uint32_t c_hi, uint32_t ib, uint32_t n,
                                               DevState* st, Best5& bs) {
     static_assert(G % 4 == 0 && kWin6 % G == 0, "groups are float4-aligned inside windows");
@@ -230,24 +292,43 @@ __device__ __forceinline__ void walk_columns6(RowBlock6<R>& rb, const ColTile6& 
     uint32_t c = c_first;
     uint64_t gk = kNoMove;  // read at the end of the previous window
     while (c < c_hi) {
-        const uint32_t w = (c - col0) / kWin6;
-        const uint32_t wend = min(c_hi, col0 + (w + 1) * kWin6);
-        const float emax = wmax[w];
-        window6<R>(rb, emax);
-        bs.busy = false;
-        const uint32_t peel_end = min(wend, ib + R + 1);
-        for (; c < peel_end; ++c) column6<R, true>(rb, t, c - col0, c, ib, emax, bs);
-        for (; c < wend && ((c - col0) & 3u); ++c)
-            column6<R, false>(rb, t, c - col0, c, ib, emax, bs);
-        for (; c + G <= wend; c += G) {
-            if (group6<R, G>(rb, t, c - col0)) {
-                bs.busy = true;
-#pragma unroll 1
-                for (uint32_t k = 0; k < G; ++k)
-                    column6<R, false>(rb, t, c + k - col0, c + k, ib, emax, bs);
-            }
+        uint32_t w = (c - col0) / kWin6;
+        if (BOX) {  // next window of the mask (earlier windows stay published)
+            const uint32_t rest = w < 32 ? (mask >> w) : 0u;
+            if (!rest) break;
+            w += __ffs(rest) - 1;
+            c = max(c, col0 + w * kWin6);
         }
-        for (; c < wend; ++c) column6<R, false>(rb, t, c - col0, c, ib, emax, bs);
+        const uint32_t wend = min(c_hi, col0 + (w + 1) * kWin6);
+        const float emax = BOX ? __ldg(wmax + w) : wmax[w];
+        bs.busy = false;
+        bool open = true;
+        if (BOX) {
+            const float4 box = __ldg(wbox + w);
+            open = box_block6<R>(rb, box, emax);
+            if (open) {
+                window6<R>(rb, emax);
+                open = box_rows6<R>(rb, box);
+            }
+        } else {
+            window6<R>(rb, emax);
+        }
+        if (open) {
+            const uint32_t peel_end = min(wend, ib + R + 1);
+            for (; c < peel_end; ++c) column6<R, true>(rb, t, c - col0, c, ib, emax, bs);
+            for (; c < wend && ((c - col0) & 3u); ++c)
+                column6<R, false>(rb, t, c - col0, c, ib, emax, bs);
+            for (; c + G <= wend; c += G) {
+                if (group6<R, G>(rb, t, c - col0)) {
+                    bs.busy = true;
+#pragma unroll 1
+                    for (uint32_t k = 0; k < G; ++k)
+                        column6<R, false>(rb, t, c + k - col0, c + k, ib, emax, bs);
+                }
+            }
+            for (; c < wend; ++c) column6<R, false>(rb, t, c - col0, c, ib, emax, bs);
+        }
+        c = wend;
         if (bs.B < bs.G) {
             atomicMin(&st->best_key, (unsigned long long)bs.best);
             bs.G = bs.B;

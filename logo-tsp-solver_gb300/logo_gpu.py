@@ -27,6 +27,7 @@ SWEEP_SQUARED = 2
 SWEEP_SQUARED_PACKED = 3
 SWEEP_FUSED = 4
 SWEEP_LOCAL = 5
+SWEEP_BOXED = 6
 DESCENT_AUTO = 0
 DESCENT_GRAPH = 1
 DESCENT_COOPERATIVE = 2
@@ -359,7 +360,7 @@ class Solver:
         return {k: getattr(i, k) for k, _ in CtxInfo._fields_}
 
     def set_kernel(self, variant, rows_per_thread, warps_per_cta, tile_cols):
-        """Variant (SWEEP_MUFU .. SWEEP_LOCAL) and tile shape."""
+        """Variant (SWEEP_MUFU .. SWEEP_BOXED) and tile shape."""
         _check(load().logo_ctx_set_kernel(self._h, variant, rows_per_thread, warps_per_cta,
                                           tile_cols), self._h)
 

@@ -62,13 +62,15 @@ KERNELS = [(2, 2, 2, 64), (2, 4, 2, 128), (2, 4, 4, 64), (2, 8, 4, 1024), (2, 8,
            (4, 4, 2, 64), (4, 4, 4, 64), (4, 4, 8, 256), (4, 8, 2, 128), (4, 8, 4, 512),
            (4, 8, 8, 100), (4, 16, 4, 1024),
            (5, 4, 2, 64), (5, 4, 4, 64), (5, 4, 8, 256), (5, 8, 4, 512), (5, 8, 8, 100),
-           (5, 16, 4, 1024)]
+           (5, 16, 4, 1024),
+           (6, 4, 2, 64), (6, 4, 4, 64), (6, 4, 8, 256), (6, 8, 4, 512), (6, 8, 8, 96),
+           (6, 16, 4, 1024), (6, 4, 4, 32)]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
 def test_every_tile_shape(lg, inst, oracle_mod, kernel):
-    """Every sweep variant (MUFU, packed MUFU, squared, packed squared and
-    fused screens) and every tile shape choose the oracle's move."""
+    """Every sweep variant (MUFU, packed MUFU, squared, packed squared, fused,
+    local and boxed screens) and every tile shape choose the oracle's move."""
     for n, seed in ((3001, 1), (777, 2), (70, 3)):
         xy = _instance(inst, n, seed)
         r = inst.random_tour(n, seed)
@@ -85,7 +87,7 @@ def test_every_tile_shape(lg, inst, oracle_mod, kernel):
             assert np.array_equal(got, want), kernel
 
 
-VARIANTS = [(v, 8, 4, 128) for v in range(6)]
+VARIANTS = [(v, 8, 4, 128) for v in range(7)]
 
 
 @pytest.mark.parametrize("kernel", VARIANTS)
@@ -339,7 +341,9 @@ def test_device_waits_give_up_then_context_usable(lg, inst, oracle_mod):
 
 GROUPED_KERNELS = [(4, 4, 4, 256), (4, 4, 2, 256), (4, 4, 8, 128), (4, 8, 4, 512), (4, 8, 8, 256),
                    (4, 16, 4, 1024), (5, 4, 4, 256), (5, 4, 2, 256), (5, 4, 8, 128),
-                   (5, 8, 4, 512), (5, 8, 8, 256), (5, 16, 4, 1024)]
+                   (5, 8, 4, 512), (5, 8, 8, 256), (5, 16, 4, 1024), (6, 4, 4, 256),
+                   (6, 4, 2, 256), (6, 4, 8, 128), (6, 8, 4, 512), (6, 8, 8, 256),
+                   (6, 16, 4, 1024), (6, 4, 4, 32)]
 
 
 def test_grouped_paths_late_descent(lg, inst, oracle_mod):
@@ -368,9 +372,11 @@ def test_grouped_paths_late_descent(lg, inst, oracle_mod):
                                            (100000, "clustered_nn", 2),
                                            (100000, "clustered_nn", 4),
                                            (100000, "clustered_nn", 5),
+                                           (100000, "clustered_nn", 6),
                                            (200000, "uniform_random", None),
                                            (200000, "uniform_random", 4),
-                                           (200000, "uniform_random", 5)])
+                                           (200000, "uniform_random", 5),
+                                           (200000, "uniform_random", 6)])
 def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen, variant):
     """Full-size single sweeps against the oracle's multi-threaded sweep
     (default kernel and the square-root-free screens)."""
@@ -386,3 +392,38 @@ def test_large_sweep_matches_parallel_oracle(lg, inst, oracle_mod, n, gen, varia
         if variant is not None:
             s.set_kernel(variant, 8, 4, 512)
         assert s.optimize_step(r) == oracle_mod.unpack_key(key)
+
+
+@pytest.mark.parametrize("n,seed", [(30000, 41), (60000, 42)])
+def test_full_descent_same_tour_every_large_variant(lg, inst, n, seed):
+    """Whole descents from NN start tours at full size (thousands of sweeps,
+    each late sweep with no improving move): the fused, local and boxed
+    screens reach the same tour by the same number of moves as the MUFU
+    screen, whose single steps are checked against the oracle above."""
+    xy = inst.clustered(n, seed, side=1.0e6, clusters=n // 500, sigma_frac=0.01)
+    r = lg.nn_tour(xy, 0)
+    out = []
+    for kernel in ((0, 4, 4, 128), (4, 4, 4, 512), (5, 4, 4, 512), (6, 4, 4, 512),
+                   (6, 8, 8, 1024)):
+        with lg.Solver(xy) as s:
+            s.set_kernel(*kernel)
+            got, st = s.optimize(r)
+        out.append((kernel, got, st["moves"], st["final_length"]))
+    for kernel, got, m, length in out[1:]:
+        assert np.array_equal(got, out[0][1]), kernel
+        assert (m, length) == (out[0][2], out[0][3]), kernel
+
+
+def test_boxed_variant_tile_widths(lg, inst):
+    """The boxed screen takes tile widths that are multiples of 32 up to 1024
+    (one mask bit per 32-column window) and rejects the others."""
+    xy = inst.uniform_f32(500, 3, 1.0e4)
+    with lg.Solver(xy) as s:
+        for cb in (100, 2048, 48):
+            with pytest.raises(lg.LogoError) as e:
+                s.set_kernel(lg.SWEEP_BOXED, 4, 4, cb)
+            assert e.value.status == 1
+        s.set_kernel(lg.SWEEP_BOXED, 4, 4, 1024)
+        with pytest.raises(lg.LogoError):
+            s.set_shape(4, 4, 1000)
+        assert s.info()["variant"] == lg.SWEEP_BOXED and s.info()["tile_cols"] == 1024

@@ -477,7 +477,8 @@ logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
  *   tiles with a (32-row window, 32-column window) pair whose box distance
  *   lets some pair be chosen; (3) a persistent sweep over the kept tiles
  *   that tests each thread's rows against each window's box with the live
- *   best delta before running the local screen on what is left.  Tile
+ *   best delta and evaluates what is left pair by pair, one lane per column
+ *   (or, on tiles where most rows are open, with the local screen).  Tile
  *   widths must be multiples of 32 up to 1024. */
 #define LOGO_SWEEP_MUFU 0
 #define LOGO_SWEEP_MUFU_PACKED 1

@@ -33,7 +33,6 @@ struct logo_ctx {
     uint32_t* d_route_best = nullptr;
     DevState* d_st = nullptr;
     DevState* h_st = nullptr;  // pinned mirror
-    uint32_t* h_route = nullptr;  // pinned staging
     uint32_t* d_seen = nullptr;   // bitmap of the route permutation check
     float4* d_wbox = nullptr;     // per-window boxes and largest edges (boxed sweep)
     float* d_wmax = nullptr;
@@ -125,14 +124,14 @@ uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) /
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
     // measured on GB300 (one sweep: NN start tours of Gaussian mixtures, the
     // local optimum of the n = 100k one, uniform points on random tours): from
-    // n = 17.5k up the boxed screen is fastest (n = 100k NN tour: 0.107 ms with
-    // (4, 4, 256) tiles vs 0.61 local, 0.83 fused, 1.80 MUFU; at its local
-    // optimum 0.144 vs 0.68; random tour 0.33 vs 0.68, 0.27 with 512-column
-    // tiles; n = 40k: 0.068 ms with 64-column tiles vs 0.087 with 256 and
-    // 0.149 local; n = 20k: 0.064 vs 0.067 local and 0.084 MUFU; n = 1M random
-    // tour: 8.5 ms with (8, 8, 1024) vs 54.8 local); below it the MUFU screen,
+    // n = 17.5k up the boxed screen is fastest (n = 100k NN tour: 0.090 ms with
+    // (4, 4, 128) tiles vs 0.61 local, 0.83 fused, 1.80 MUFU; at its local
+    // optimum 0.109 vs 0.68; random tour 0.39 vs 0.68, 0.23 with (8, 8, 1024)
+    // tiles; n = 40k: 0.063 ms with 64-column tiles vs 0.078 with 128 and
+    // 0.149 local; n = 20k: 0.067 vs 0.067 local and 0.084 MUFU; n = 1M random
+    // tour: 7.1 ms with (8, 8, 1024) vs 54.8 local); below it the MUFU screen,
     // whose test is tighter on short tours, wins, with 64-column tiles from 3k
-    // (n = 10k: 0.030 ms vs 0.059 boxed and 0.042 with (4, 4, 128) MUFU tiles).
+    // (n = 10k: 0.030 ms vs 0.063 boxed and 0.042 with (4, 4, 128) MUFU tiles).
     variant = LOGO_SWEEP_MUFU;
     if (n >= 300000) {
         variant = LOGO_SWEEP_BOXED;
@@ -140,9 +139,6 @@ void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
     } else if (n >= 200000) {
         variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 512;
-    } else if (n >= 80000) {
-        variant = LOGO_SWEEP_BOXED;
-        R = 4; NW = 4; cb = 256;
     } else if (n >= 50000) {
         variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 128;
@@ -236,10 +232,12 @@ logo_status rebuild(logo_ctx* c) {
 // check cost about 80 us per call at n = 100k, a tenth of a sweep);
 // read_state reports a bad route as LOGO_ERR_INVALID_ARG, and a descent on
 // it converges before any sweep.
+// The route is copied straight from and to the caller's buffer: measured on
+// GB300 (n = 100k, 400 KB) 11 us each way, against 19 us (in) and 23 us
+// (out) through a pinned staging buffer and a host memcpy.
 logo_status upload_route(logo_ctx* c, const uint32_t* route) {
     if (!route) return fail(c, LOGO_ERR_INVALID_ARG, "route is NULL");
-    std::memcpy(c->h_route, route, sizeof(uint32_t) * c->n);
-    CK(c, cudaMemcpyAsync(c->d_route[0], c->h_route, sizeof(uint32_t) * c->n,
+    CK(c, cudaMemcpyAsync(c->d_route[0], route, sizeof(uint32_t) * c->n,
                           cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaMemsetAsync(c->d_seen, 0, sizeof(uint32_t) * ((c->n + 31) / 32), c->stream));
     CK(c, cudaMemsetAsync(&c->d_st->bad_route, 0, sizeof(unsigned int), c->stream));
@@ -366,10 +364,9 @@ logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t 
 
 logo_status download_route(logo_ctx* c, uint32_t* route, bool best) {
     const uint32_t* src = best ? c->d_route_best : c->d_route[c->h_st->cur & 1];
-    CK(c, cudaMemcpyAsync(c->h_route, src, sizeof(uint32_t) * c->n,
-                          cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(route, src, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToHost,
+                          c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    std::memcpy(route, c->h_route, sizeof(uint32_t) * c->n);
     return LOGO_OK;
 }
 
@@ -404,7 +401,6 @@ void destroy(logo_ctx* c) {
     cudaFree(c->d_workctl);
     cudaFree(c->d_coop);
     if (c->h_st) cudaFreeHost(c->h_st);
-    if (c->h_route) cudaFreeHost(c->h_route);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -516,7 +512,6 @@ logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_
     CKC(cudaMalloc(&c->d_route_best, sizeof(uint32_t) * n));
     CKC(cudaMalloc(&c->d_st, sizeof(DevState)));
     CKC(cudaMallocHost(&c->h_st, sizeof(DevState)));
-    CKC(cudaMallocHost(&c->h_route, sizeof(uint32_t) * n));
     CKC(cudaMalloc(&c->d_seen, sizeof(uint32_t) * ((n + 31) / 32)));
     CKC(cudaMalloc(&c->d_wbox, sizeof(float4) * sweep_windows(n)));
     CKC(cudaMalloc(&c->d_wmax, sizeof(float) * sweep_windows(n)));

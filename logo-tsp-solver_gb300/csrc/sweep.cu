@@ -32,6 +32,7 @@
 #include "sweep_core4.cuh"
 #include "sweep_core5.cuh"
 #include "sweep_core6.cuh"
+#include "sweep_core7.cuh"
 
 namespace logo {
 
@@ -225,6 +226,7 @@ __global__ void __launch_bounds__(NW * 32)
 // 0.834 ms vs 0.850 with G = 8 and 0.899 ungrouped; G = 8 for 8-row blocks at
 // n = 1M, 70.9 ms vs 71.7 with G = 16 and 74.2 with G = 4).
 constexpr uint32_t kSweep5GroupMinN = 30000;
+constexpr uint32_t kMaxTileRows = 2048;  // NW * 32 * R of the largest shapes, (16, 4) and (8, 8)
 
 __host__ __device__ constexpr size_t sweep5_hot_offset(uint32_t cb) {
     return 96 + (size_t)(cb + 1) * sizeof(OrderedCity);
@@ -440,98 +442,139 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Boxed variant, pass 2: one warp per tile.  Lane c holds column window c
-// of the tile; for every row window r of the tile it tests whether some
-// pair of (row window r) x (column window c) can be chosen with B = -1, the
-// largest best delta a sweep can end with (box_block6 with the windows'
-// boxes and u = -1 + E_r + 5 + E_c, which bounds every V + 5 of those
-// pairs).  Tiles with a passing pair are appended to the work list as
-// (row0, col0, mask of their column windows that passed).
+// Boxed variant, pass 2: gridDim.y CTAs per row block (the rows of one tile
+// row, rows_per_tile of them from row0 = 1 + rows_per_tile * blockIdx.x).
+// The block's row-window statistics go to shared memory; each warp then
+// takes 32 consecutive column windows of the block at a time (lane = column
+// window, 32 / (cb / 32) tiles per step; the CTAs of a row block split its
+// steps) and tests them against every row window with B = -1, the largest best delta a sweep can end with
+// (box_gap_pass with u = -1 + E_r + 5 + E_c, which bounds every V + 5 of
+// those pairs).  Tiles with a passing pair are appended to the work list as
+// (row0, col0, mask of their column windows that passed).  The tiles are
+// the ones the tile list holds: columns from row0 + 2 to n - 1 in steps of
+// cb.
 __global__ void __launch_bounds__(256)
-    tile_filter_kernel(const uint2* __restrict__ tiles, uint32_t ntiles, uint32_t n,
-                       uint32_t rows_per_tile, uint32_t cb, const float4* __restrict__ wbox,
-                       const float* __restrict__ wmax, const float4* __restrict__ rbox,
-                       const float* __restrict__ rmax, uint4* __restrict__ work,
-                       uint32_t* __restrict__ workctl, DevState* st) {
+    tile_filter_kernel(uint32_t n, uint32_t rows_per_tile, uint32_t cb,
+                       const float4* __restrict__ wbox, const float* __restrict__ wmax,
+                       const float4* __restrict__ rbox, const float* __restrict__ rmax,
+                       uint4* __restrict__ work, uint32_t* __restrict__ workctl, DevState* st) {
+    __shared__ float4 srb[kMaxTileRows / kWin6];
+    __shared__ float sre[kMaxTileRows / kWin6];
     if (*(volatile unsigned int*)&st->converged) return;
-    const uint32_t t = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (t >= ntiles) return;  // whole warps
-    const uint2 tile = tiles[t];
-    const uint32_t row0 = tile.x, col0 = tile.y;
+    const uint32_t row0 = 1 + blockIdx.x * rows_per_tile;
+    const uint32_t ntiles = (n - row0 - 2 + cb - 1) / cb;  // columns row0 + 2 .. n - 1
+    const uint32_t wpt = cb / kWin6;                       // windows per tile (cb % 32 == 0)
+    const uint32_t tps = 32u / wpt;                        // tiles per step
+    if (blockIdx.y * 8 * tps >= ntiles) return;            // the whole CTA
     const uint32_t row_end = min(row0 + rows_per_tile, n - 2);  // rows i + 3 <= n
-    const uint32_t col_end = min(col0 + cb, n);
     const uint32_t nrw = (row_end - row0 + kWin6 - 1) / kWin6;
-    const uint32_t ncw = (col_end - col0 + kWin6 - 1) / kWin6;  // <= 32
-    const bool has_col = lane < ncw;
-    const uint32_t cw = (col0 - 3) / kWin6 + (has_col ? lane : 0);
-    const float4 cbx = wbox[cw];
-    const float ce = wmax[cw];
-    const uint32_t last_col = min(col0 + (lane + 1) * kWin6, col_end) - 1;
     const uint32_t rw0 = (row0 - 1) / kWin6;
-    bool any = false;
-    for (uint32_t base = 0; base < nrw; base += 32) {
-        // lane k loads row window base + k; the loop broadcasts them
-        const uint32_t nr = min(32u, nrw - base);
-        const uint32_t rw = rw0 + base + (lane < nr ? lane : 0);
-        const float4 rbl = rbox[rw];
-        const float rel = rmax[rw];
-        for (uint32_t r = 0; r < nr; ++r) {
-            const float4 rb = make_float4(__shfl_sync(0xffffffffu, rbl.x, r),
-                                          __shfl_sync(0xffffffffu, rbl.y, r),
-                                          __shfl_sync(0xffffffffu, rbl.z, r),
-                                          __shfl_sync(0xffffffffu, rbl.w, r));
-            const float re = __shfl_sync(0xffffffffu, rel, r);
-            if (!has_col || last_col < row0 + (base + r) * kWin6 + 2) continue;  // no c >= i + 2
-            const float u = (re + 4.f) + ce;
-            const float gx = fmaxf(fmaxf(__fsub_rn(cbx.x, rb.y), __fsub_rn(rb.x, cbx.y)), 0.f);
-            const float gy = fmaxf(fmaxf(__fsub_rn(cbx.z, rb.w), __fsub_rn(rb.z, cbx.w)), 0.f);
-            const float s = __fmaf_rn(gy, gy, __fmul_rn(gx, gx));
-            any |= u > 0.f && s < __fmul_rn(u, u);
+    for (uint32_t r = threadIdx.x; r < nrw; r += blockDim.x) {
+        srb[r] = rbox[rw0 + r];
+        sre[r] = rmax[rw0 + r];
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t col_start = row0 + 2;
+    for (uint32_t t0 = (blockIdx.y * 8 + warp) * tps; t0 < ntiles; t0 += gridDim.y * 8 * tps) {
+        const uint32_t tk = t0 + lane / wpt;
+        const uint32_t col = col_start + tk * cb + (lane % wpt) * kWin6;  // window start
+        bool any = false;
+        if (tk < ntiles && lane < tps * wpt && col < n) {
+            const uint32_t cw = (col - 3) / kWin6;
+            const float4 cbx = wbox[cw];
+            const float ce = wmax[cw];
+            const uint32_t last_col = min(col + kWin6, n) - 1;
+            for (uint32_t r = 0; r < nrw; ++r) {
+                if (last_col < row0 + r * kWin6 + 2) break;  // no pair c >= i + 2 from here on
+                if (box_gap_pass(srb[r], cbx, (sre[r] + 4.f) + ce)) {
+                    any = true;
+                    break;
+                }
+            }
+        }
+        const uint32_t votes = __ballot_sync(0xffffffffu, any);
+        if (lane < tps && t0 + lane < ntiles) {
+            const uint32_t mask =
+                (votes >> (lane * wpt)) & (wpt == 32 ? 0xffffffffu : ((1u << wpt) - 1u));
+            if (mask)
+                work[atomicAdd(&workctl[0], 1u)] =
+                    make_uint4(row0, col_start + (t0 + lane) * cb, mask, 0u);
         }
     }
-    const uint32_t mask = __ballot_sync(0xffffffffu, any);
-    if (lane == 0 && mask) work[atomicAdd(&workctl[0], 1u)] = make_uint4(row0, col0, mask, 0u);
 }
 
-// Boxed variant, pass 3 (LOGO_SWEEP_BOXED): a persistent grid takes the work
-// list's tiles one at a time.  Per tile: the local-coordinate screen of
-// sweep_kernel6, where each thread first tests the bounding box of its rows
-// against the passing windows' boxes with its current B (box_block6); only
-// the column range of windows some thread can use is staged (one bulk copy)
-// and converted.  Tile columns start at 3 + 32k (tile widths are multiples of
-// 32) and rows at 1 + 32k, so tile window w is window (col0 - 3) / 32 + w of
-// pass 1.  The best delta found carries over from tile to tile and is
-// tightened with the sweep's shared best at every claim (a random tour's
-// large improvements are found by the first tiles; without the refresh a
-// CTA kept the B it started with).  A CTA claims its next item only when it
-// is free (claiming ahead left items
-// reserved by busy CTAs while others ran out: n = 100k local optimum 0.20 ms
-// vs 0.16).
+// Boxed variant, pass 3 (LOGO_SWEEP_BOXED, sweep_core7.cuh): a persistent
+// grid takes the work list's tiles one at a time.  Per tile, each thread
+// loads its R rows and, for every window the filter kept, runs the block
+// test and the one-row tests with its current B; what passes goes into a
+// queue of units (thread, window, rows) in shared memory.  Only tiles with
+// units stage their columns (one bulk copy of the range the units touch).
+// A tile with few units has its warps take them round robin, one lane per
+// column, so the rare open blocks are spread over the CTA and no lane idles
+// on a closed one.  A tile whose units would keep most lanes busy is walked
+// the way sweep_kernel6 walks a tile instead, every thread over its open
+// windows with the local-coordinate screen, which is cheaper per pair when
+// most lanes have work: a warp walks for as long as its busiest lane, each
+// open window costing about as much as kWalkRows open rows of units, so the
+// tile is walked when its open rows exceed kWalkRows x R x (sum over warps
+// of the busiest lane's open windows).
+// Tile columns start at 3 + 32k (tile widths are multiples of 32) and rows
+// at 1 + 32k, so tile window w is window (col0 - 3) / 32 + w of pass 1.  B
+// carries over from tile to tile, is tightened with the sweep's shared best
+// at every claim and shared within a warp after every unit.  A CTA claims
+// its next item only when it is free (claiming ahead left items reserved by
+// busy CTAs while others ran out).
 struct BoxedSlot {
     uint32_t idx;
-    uint32_t need;            // windows some thread of the CTA may use
+    uint32_t need;            // windows the units touch
     unsigned long long best;  // the sweep's best key when the item was claimed
     uint4 item;               // row0, col0, column-window mask
+    uint32_t units;           // units queued
+    uint32_t walk;            // sum over warps of the most windows one lane opened
+    uint32_t rows;            // open rows over all units
 };
-
-// Resident CTAs per SM the boxed kernel is compiled for (register budget):
-// 4-row, 4-warp CTAs at 96 registers fit 5 per SM (measured faster than 4
-// at 125 registers); the other shapes keep about their unconstrained counts.
-constexpr int boxed_min_blocks(int R, int NW) {
-    return R == 4 ? (NW == 4 ? 5 : NW == 8 ? 2 : 8) : R == 8 ? 2 : 1;
+// Open rows of units that take as long as walking one window per row of a
+// thread (measured on GB300, n = 100k, (4, 4, 128) tiles: NN start tour
+// 0.090 ms and its local optimum 0.109 ms with 16; 0.093 / 0.126 with 8;
+// 0.135 / 0.107 with 32; walking every tile with a unit 0.094 / 0.130).
+constexpr uint32_t kWalkRows = 16;
+constexpr size_t kBoxedStageOffset = 96;
+__host__ __device__ constexpr size_t boxed_queue_offset(uint32_t cb) {
+    return kBoxedStageOffset + (((size_t)cb + 1) * sizeof(OrderedCity) + 15) / 16 * 16;
+}
+__host__ __device__ constexpr size_t boxed_cx_offset(uint32_t cb, int NW) {
+    return boxed_queue_offset(cb) + (size_t)NW * 32 * (cb / kWin7) * sizeof(uint32_t);
+}
+__host__ __device__ constexpr size_t boxed_smem_bytes(uint32_t cb, int NW) {
+    return boxed_cx_offset(cb, NW) + 3 * sweep6_cols4(cb) * sizeof(float);
 }
 
-template <int R, int NW, int G>
+// Resident CTAs per SM the boxed kernel is compiled for (register budget:
+// 4-row threads at 96 registers, 8-row threads at 128).
+constexpr int boxed_min_blocks(int R, int NW) {
+    return R == 4 ? (NW == 2 ? 10 : NW == 4 ? 5 : 2) : R == 8 ? (NW == 8 ? 2 : 4) : 1;
+}
+
+__device__ __forceinline__ int warp_min_int(int v) {
+    for (int o = 16; o; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <int R, int NW>
 __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
     sweep_boxed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                        uint32_t n, uint32_t cb, const float4* __restrict__ gbox,
                        const float* __restrict__ gmax, const uint4* __restrict__ work,
                        uint32_t* __restrict__ workctl, DevState* st) {
+    static_assert(R <= 16 && NW * 32 <= 256, "unit encoding: 8-bit thread, 16-bit rows");
+    constexpr int G = (128 / R) < 32 ? (128 / R) : 32;
     extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    BoxedSlot* slot = reinterpret_cast<BoxedSlot*>(smem_raw + 48);  // 32 bytes
-    OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
-    float* cx = reinterpret_cast<float*>(smem_raw + sweep6_cx_offset(cb));
+    BoxedSlot* slot = reinterpret_cast<BoxedSlot*>(smem_raw + 16);  // 48 bytes
+    OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + kBoxedStageOffset);
+    uint32_t* queue = reinterpret_cast<uint32_t*>(smem_raw + boxed_queue_offset(cb));
+    float* cx = reinterpret_cast<float*>(smem_raw + boxed_cx_offset(cb, NW));
     float* cy = cx + sweep6_cols4(cb);
     float* cc = cy + sweep6_cols4(cb);
 
@@ -557,6 +600,9 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
             const uint32_t idx = atomicAdd(&workctl[1], 1u);
             slot->idx = idx;
             slot->need = 0u;
+            slot->units = 0u;
+            slot->walk = 0u;
+            slot->rows = 0u;
             slot->best = *(volatile unsigned long long*)&st->best_key;
             if (idx < items) slot->item = work[idx];
         }
@@ -567,66 +613,96 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
             const uint64_t gk = slot->best;
             if (gk != kNoMove) {
                 const int g = key_delta(gk);
-                if (g < bs.B) bs.B = g;
-                if (g < bs.G) bs.G = g;
+                bs.B = min(bs.B, g);
+                bs.G = min(bs.G, g);
             }
         }
         const uint32_t row0 = item.x, col0 = item.y;
         const uint32_t col_end = min(col0 + cb, n);
-        const float4* tbox = gbox + (col0 - 3) / kWin6;
-        const float* tmax = gmax + (col0 - 3) / kWin6;
-        const uint32_t ib = row0 + (warp * 32 + lane) * R;
-        bs.busy = false;
-        const OrderedCity origin = Q[row0];  // same for every thread of the tile
-        RowBlock6<R> rb;
-        load_rows6<R>(rb, Q, ib, n, origin.x, origin.y);
-        refresh6<R>(rb, Q, ib, n, bs.B);
-        uint32_t mask = 0;  // windows this thread's rows may use
+        const float4* tbox = gbox + (col0 - 3) / kWin7;
+        const float* tmax = gmax + (col0 - 3) / kWin7;
+        const uint32_t ib = row0 + threadIdx.x * R;
+        uint32_t open = 0;  // windows in which some row of this thread is open
+        uint32_t rows = 0;  // open rows over this thread's units
         if (ib + 3 <= n) {
+            RowBlock7<R> rb;
+            load_rows7<R>(rb, Q, ib, n, bs.B);
             for (uint32_t m = item.z; m; m &= m - 1) {
                 const uint32_t w = __ffs(m) - 1;
-                if (col0 + (w + 1) * kWin6 <= ib + 2) continue;  // left of the first pair
-                if (box_block6<R>(rb, __ldg(tbox + w), __ldg(tmax + w))) mask |= 1u << w;
+                if (col0 + (w + 1) * kWin7 <= ib + 2) continue;  // left of the first pair
+                const uint32_t rm = rows_open7<R>(rb, __ldg(tbox + w), __ldg(tmax + w));
+                if (rm) {
+                    queue[atomicAdd(&slot->units, 1u)] = (threadIdx.x << 24) | (w << 16) | rm;
+                    open |= 1u << w;
+                    rows += __popc(rm);
+                }
+            }
+            if (open) atomicOr(&slot->need, open);
+        }
+        {
+            const uint32_t busiest = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(open));
+            const uint32_t wrows = __reduce_add_sync(0xffffffffu, rows);
+            if (lane == 0 && busiest) {
+                atomicAdd(&slot->walk, busiest);
+                atomicAdd(&slot->rows, wrows);
             }
         }
-        if (mask) atomicOr(&slot->need, mask);
         __syncthreads();
-        const uint32_t all = slot->need;
-        bool ok = true;
-        if (all) {  // the same for every thread
+        const uint32_t units = slot->units, all = slot->need;
+        if (units) {  // the same for every thread
             const uint32_t wlo = __ffs(all) - 1, whi = 31 - __clz(all);
             // stage[k] = column col0 - 1 + k for k in [k0, k1)
-            const uint32_t k0 = wlo * kWin6, k1 = min((whi + 1) * kWin6, col_end - col0) + 1;
+            const uint32_t k0 = wlo * kWin7, k1 = min((whi + 1) * kWin7, col_end - col0) + 1;
             if (threadIdx.x == 0) {
                 const uint32_t bytes = (k1 - k0) * (uint32_t)sizeof(OrderedCity);
                 fence_proxy_async_smem();
                 mbar_arrive_expect_tx(bar, bytes);
                 bulk_g2s(stage + k0, Q + (col0 - 1 + k0), bytes, bar);
             }
-            ok = mbar_wait_bounded(bar, parity, &st->status);
+            const bool ok = mbar_wait_bounded(bar, parity, &st->status);
             parity ^= 1u;
-            if (ok) {
-                for (uint32_t k = k0 + 1 + threadIdx.x; k < k1; k += NW * 32) {
-                    const OrderedCity q = stage[k];
-                    const float p = __fsub_rn(q.x, origin.x), qq = __fsub_rn(q.y, origin.y);
-                    cx[k - 1] = p;
-                    cy[k - 1] = qq;
-                    cc[k - 1] = __fmaf_rn(qq, qq, __fmul_rn(p, p));
+            if (slot->rows > kWalkRows * R * slot->walk) {  // the same for every thread
+                const OrderedCity origin = Q[row0];
+                if (ok) {
+                    for (uint32_t k = k0 + 1 + threadIdx.x; k < k1; k += NW * 32) {
+                        const OrderedCity q = stage[k];
+                        const float p = __fsub_rn(q.x, origin.x), qq = __fsub_rn(q.y, origin.y);
+                        cx[k - 1] = p;
+                        cy[k - 1] = qq;
+                        cc[k - 1] = __fmaf_rn(qq, qq, __fmul_rn(p, p));
+                    }
+                }
+                // a copy that did not arrive ends the CTA's work (status has the timeout)
+                if (__syncthreads_or(!ok)) break;
+                if (open) {
+                    RowBlock6<R> rb;
+                    load_rows6<R>(rb, Q, ib, n, origin.x, origin.y);
+                    refresh6<R>(rb, Q, ib, n, bs.B);
+                    const ColTile6 t{cx, cy, cc, stage};
+                    walk_columns6<R, G, true>(rb, t, tmax, tbox, open, col0, col0, col_end, ib, n,
+                                              st, bs);
+                }
+            } else {
+                if (__syncthreads_or(!ok)) break;
+                for (uint32_t u = warp; u < units; u += NW) {
+                    const uint32_t e = queue[u];
+                    const uint32_t uib = row0 + (e >> 24) * R, w = (e >> 16) & 0xffu;
+                    const uint32_t c = col0 + w * kWin7 + lane;
+                    if (c < col_end) unit7<R>(Q, stage, col0, c, uib, e & 0xffffu, n, bs.B, bs.best);
+                    bs.B = warp_min_int(bs.B);
+                    if (bs.B < bs.G) {  // publish the warp's best
+                        const uint64_t k = warp_min_u64(bs.best);
+                        if (lane == 0) atomicMin(&st->best_key, (unsigned long long)k);
+                        bs.G = bs.B;
+                    }
                 }
             }
-            // a copy that did not arrive ends the CTA's work (status has the timeout)
-            if (__syncthreads_or(!ok)) break;
-            if (mask) {
-                const ColTile6 t{cx, cy, cc, stage};
-                walk_columns6<R, G, true>(rb, t, tmax, tbox, mask, col0, col0, col_end, ib, n,
-                                          st, bs);
-            }
         }
-        __syncthreads();  // every thread has read the slot and the tile's shared memory
+        __syncthreads();  // every thread has read the slot, the queue and the stage
     }
 
-    const uint64_t best = warp_min_u64(bs.best);
-    if (lane == 0 && best != kNoMove) atomicMin(&st->best_key, (unsigned long long)best);
+    const uint64_t k = warp_min_u64(bs.best);
+    if (lane == 0 && k != kNoMove) atomicMin(&st->best_key, (unsigned long long)k);
 }
 
 __host__ __device__ constexpr size_t sweep2_cols_offset(uint32_t cb) {
@@ -770,35 +846,8 @@ size_t sweep6_smem_bytes(uint32_t cb) {
     return sweep6_wmax_offset(cb) + ((size_t)cb / kWin6 + 2) * sizeof(float);
 }
 
-template <int R, int NW, int G, bool BOX>
+template <int R, int NW, int G>
 static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool prepare) {
-    if (BOX) {
-        // stage and column arrays only; the window statistics stay in global memory
-        const size_t smem = sweep6_wmax_offset(L.cb);
-        if (prepare) {
-            return cudaFuncSetAttribute(sweep_boxed_kernel<R, NW, G>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        attr_bytes(sweep6_wmax_offset(kMaxBoxedCols)));
-        }
-        int device = 0, sms = 0, per_sm = 0;
-        cudaError_t e = cudaGetDevice(&device);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_boxed_kernel<R, NW, G>,
-                                                              NW * 32, smem);
-        if (e != cudaSuccess) return e;
-        const uint32_t resident = (uint32_t)(per_sm > 0 ? per_sm : 1) * (uint32_t)sms;
-        const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
-        const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
-        window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.n, L.wbox, L.wmax,
-                                                           L.rbox, L.rmax, L.workctl, L.st);
-        tile_filter_kernel<<<(L.ntiles + 7) / 8, 256, 0, s>>>(
-            L.tiles, L.ntiles, L.n, (uint32_t)(NW * 32 * R), L.cb, L.wbox, L.wmax, L.rbox,
-            L.rmax, L.work, L.workctl, L.st);
-        sweep_boxed_kernel<R, NW, G><<<grid, NW * 32, smem, s>>>(
-            L.Q0, L.Q1, L.n, L.cb, L.wbox, L.wmax, L.work, L.workctl, L.st);
-        return cudaGetLastError();
-    }
     const size_t smem = sweep6_smem_bytes(L.cb);
     if (prepare) {
         return cudaFuncSetAttribute(sweep_kernel6<R, NW, G>,
@@ -810,18 +859,52 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
     return cudaGetLastError();
 }
 
+// Boxed variant: window statistics, tile filter, persistent sweep (one CTA
+// per resident slot).
+template <int R, int NW>
+static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
+    const size_t smem = boxed_smem_bytes(L.cb, NW);
+    if (prepare) {
+        return cudaFuncSetAttribute(sweep_boxed_kernel<R, NW>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    attr_bytes(boxed_smem_bytes(kMaxBoxedCols, NW)));
+    }
+    int device = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_boxed_kernel<R, NW>,
+                                                          NW * 32, smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t resident = (uint32_t)(per_sm > 0 ? per_sm : 1) * (uint32_t)sms;
+    const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
+    const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
+    window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.n, L.wbox, L.wmax, L.rbox,
+                                                       L.rmax, L.workctl, L.st);
+    const uint32_t rows_per_tile = (uint32_t)(NW * 32 * R);
+    const uint32_t row_blocks = (L.n - 4) / rows_per_tile + 1;  // row0 + 3 <= n
+    // CTAs per row block: one step per warp for the longest row (block 0)
+    const uint32_t steps = ((L.n - 3 + L.cb - 1) / L.cb + 32 / (L.cb / 32) - 1) / (32 / (L.cb / 32));
+    const dim3 fgrid(row_blocks, (steps + 7) / 8);
+    tile_filter_kernel<<<fgrid, 256, 0, s>>>(L.n, rows_per_tile, L.cb, L.wbox, L.wmax, L.rbox,
+                                             L.rmax, L.work, L.workctl, L.st);
+    sweep_boxed_kernel<R, NW><<<grid, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.cb, L.wbox, L.wmax,
+                                                          L.work, L.workctl, L.st);
+    return cudaGetLastError();
+}
+
 // Column groups of the local-coordinate screen: 128 / R columns per branch
 // (measured on GB300 with 4-row blocks: n = 100k 0.631 ms with 32 columns vs
 // 0.641 with 16; n = 1M 54.7 ms vs 55.5), 4 below kSweep5GroupMinN cities.
-template <int R, int NW, bool BOX>
+template <int R, int NW>
 static cudaError_t launch_sweep6_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     constexpr int G = (128 / R) < 32 ? (128 / R) : 32;
     if (prepare) {
-        const cudaError_t e = launch_sweep6_g<R, NW, 4, BOX>(L, s, true);
-        return e != cudaSuccess ? e : launch_sweep6_g<R, NW, G, BOX>(L, s, true);
+        const cudaError_t e = launch_sweep6_g<R, NW, 4>(L, s, true);
+        return e != cudaSuccess ? e : launch_sweep6_g<R, NW, G>(L, s, true);
     }
-    return L.n >= kSweep5GroupMinN ? launch_sweep6_g<R, NW, G, BOX>(L, s, false)
-                                   : launch_sweep6_g<R, NW, 4, BOX>(L, s, false);
+    return L.n >= kSweep5GroupMinN ? launch_sweep6_g<R, NW, G>(L, s, false)
+                                   : launch_sweep6_g<R, NW, 4>(L, s, false);
 }
 
 template <int R, int NW>
@@ -853,23 +936,23 @@ static cudaError_t launch_sweep_t(const SweepLaunch& L, cudaStream_t s, bool pre
 static cudaError_t dispatch_sweep(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     if (L.variant == 6) {
         switch (L.R * 100 + L.NW) {
-            case 402: return launch_sweep6_t<4, 2, true>(L, s, prepare);
-            case 404: return launch_sweep6_t<4, 4, true>(L, s, prepare);
-            case 408: return launch_sweep6_t<4, 8, true>(L, s, prepare);
-            case 804: return launch_sweep6_t<8, 4, true>(L, s, prepare);
-            case 808: return launch_sweep6_t<8, 8, true>(L, s, prepare);
-            case 1604: return launch_sweep6_t<16, 4, true>(L, s, prepare);
+            case 402: return launch_boxed_t<4, 2>(L, s, prepare);
+            case 404: return launch_boxed_t<4, 4>(L, s, prepare);
+            case 408: return launch_boxed_t<4, 8>(L, s, prepare);
+            case 804: return launch_boxed_t<8, 4>(L, s, prepare);
+            case 808: return launch_boxed_t<8, 8>(L, s, prepare);
+            case 1604: return launch_boxed_t<16, 4>(L, s, prepare);
             default: return cudaErrorInvalidValue;
         }
     }
     if (L.variant == 5) {
         switch (L.R * 100 + L.NW) {
-            case 402: return launch_sweep6_t<4, 2, false>(L, s, prepare);
-            case 404: return launch_sweep6_t<4, 4, false>(L, s, prepare);
-            case 408: return launch_sweep6_t<4, 8, false>(L, s, prepare);
-            case 804: return launch_sweep6_t<8, 4, false>(L, s, prepare);
-            case 808: return launch_sweep6_t<8, 8, false>(L, s, prepare);
-            case 1604: return launch_sweep6_t<16, 4, false>(L, s, prepare);
+            case 402: return launch_sweep6_t<4, 2>(L, s, prepare);
+            case 404: return launch_sweep6_t<4, 4>(L, s, prepare);
+            case 408: return launch_sweep6_t<4, 8>(L, s, prepare);
+            case 804: return launch_sweep6_t<8, 4>(L, s, prepare);
+            case 808: return launch_sweep6_t<8, 8>(L, s, prepare);
+            case 1604: return launch_sweep6_t<16, 4>(L, s, prepare);
             default: return cudaErrorInvalidValue;
         }
     }

@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(NT)
     batch_kernel(BatchArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ CtaShared<NT> S;
+    __shared__ CtaWindows W;
     __shared__ unsigned int share_flag, share_seq;
     OrderedCity* Q = reinterpret_cast<OrderedCity*>(smem_raw);
     uint32_t* route = reinterpret_cast<uint32_t*>(smem_raw + sizeof(OrderedCity) * A.max_n);
@@ -242,7 +243,9 @@ __global__ void __launch_bounds__(NT)
             // descent
             unsigned long long dm = 0;
             for (;;) {
-                const unsigned long long key = sweep<R, NT, TC>(S, Q, n, I.margin);
+                window_stats_cta<NT>(W, Q, n);
+                __syncthreads();
+                const unsigned long long key = sweep_boxed<R, NT, TC>(S, W, Q, n, I.margin);
                 ++sweeps;
                 if (key == kNoMove) break;
                 const uint32_t p = key_i(key), q = key_j(key);

@@ -11,11 +11,14 @@
 //   tour_length     ≙ routeLength, src/headers.h:170-189
 //   sweep           ≙ the CPUSolver::optimizeStep loop (src/solvers/cpuSolver.cpp:188-230)
 //                     over warp tiles of 32R rows x TC columns
+//   sweep_boxed     the same, skipping the 32-column windows that the box
+//                     test of sweep_core7.cuh closes for a lane's rows
 #pragma once
 #include <cstdint>
 
 #include "logo_device.cuh"
 #include "sweep_core.cuh"
+#include "sweep_core7.cuh"
 
 namespace logo {
 
@@ -156,6 +159,107 @@ __device__ __forceinline__ unsigned long long sweep(CtaShared<NT>& S, const Orde
     return k;
 }
 
+
+// Bounding box and largest edge of every window of 32 columns (columns
+// 3 + 32 g .. 3 + 32 g + 31, below n) of the resident tour, for
+// sweep_boxed; up to kCtaWindows windows (tours up to 4096 cities).
+constexpr uint32_t kCtaWindows = 130;
+struct CtaWindows {
+    float4 box[kCtaWindows];  // (x0, x1, y0, y1)
+    float emax[kCtaWindows];
+};
+
+template <int NT>
+__device__ __forceinline__ void window_stats_cta(CtaWindows& W, const OrderedCity* Q,
+                                                 uint32_t n) {
+    const uint32_t nwin = n < 4 ? 0u : (n - 3 + kWin7 - 1) / kWin7;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t g = threadIdx.x >> 5; g < nwin; g += NT / 32) {  // whole warps
+        const uint32_t c = 3 + g * kWin7 + lane;
+        const bool in = c < n;
+        const OrderedCity q = Q[in ? c : n - 1];
+        float m = in ? q.e : 0.f;
+        float x0 = in ? q.x : FLT_MAX, x1 = in ? q.x : -FLT_MAX;
+        float y0 = in ? q.y : FLT_MAX, y1 = in ? q.y : -FLT_MAX;
+        for (int o = 16; o; o >>= 1) {
+            m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        }
+        if (lane == 0) {
+            W.box[g] = make_float4(x0, x1, y0, y1);
+            W.emax[g] = m;
+        }
+    }
+}
+
+// sweep() with the window test: each lane walks a window of its tile only
+// when the bounding box of its rows and the window's box let some pair be
+// chosen with its current B (box_gap_pass, u = B + max e[i] + 5 + the
+// window's largest edge, which bounds every V + 5 of those pairs).  W must
+// hold the current tour's windows (window_stats_cta, then a barrier).  Tile
+// columns start at 3 + 32k (32R-row blocks, TC a multiple of 32), so every
+// window lies in one tile.
+template <int R, int NT, int TC>
+__device__ __forceinline__ unsigned long long sweep_boxed(CtaShared<NT>& S, const CtaWindows& W,
+                                                          const OrderedCity* Q, uint32_t n,
+                                                          float margin) {
+    static_assert(TC % kWin7 == 0, "tile columns start at 3 + 32k");
+    constexpr int NW = NT / 32;
+    constexpr uint32_t RT = 32 * R;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t best = kNoMove;
+    if (n >= 5) {
+        const uint32_t nrb = (n - 3 + RT - 1) / RT;  // row blocks over rows 1..n-3
+        const uint32_t total = S.tiles_before[nrb];
+        uint32_t rbk = 0;
+        for (uint32_t t = warp; t < total; t += NW) {
+            while (S.tiles_before[rbk + 1] <= t) ++rbk;
+            const uint32_t row0 = 1 + rbk * RT;
+            const uint32_t col0 = row0 + 2 + (t - S.tiles_before[rbk]) * TC;
+            const uint32_t col1 = min(col0 + TC, n);
+            const uint32_t ib = row0 + lane * R;
+            if (ib + 3 > n) continue;  // no pairs in this lane's rows
+            int B = -1;
+            RowBlock<R> rb;
+            load_rows<R>(rb, Q, ib, n);
+            refresh_thresholds<R>(rb, Q, ib, n, B, margin);
+            float emax_rows = -3.0e7f;
+            float4 box = make_float4(rb.x[1], rb.x[1], rb.y[1], rb.y[1]);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (ib + r + 3 <= n) emax_rows = fmaxf(emax_rows, Q[ib + r].e);
+                box.x = fminf(box.x, rb.x[r + 1]);
+                box.y = fmaxf(box.y, rb.x[r + 1]);
+                box.z = fminf(box.z, rb.y[r + 1]);
+                box.w = fmaxf(box.w, rb.y[r + 1]);
+            }
+            for (uint32_t c = col0; c < col1;) {
+                const uint32_t g = (c - 3) / kWin7;
+                const uint32_t wend = min(3 + (g + 1) * kWin7, col1);
+                if (wend > ib + 2 &&
+                    box_gap_pass(box, W.box[g], ((float)(B + 5) + emax_rows) + W.emax[g]))
+                    walk_columns<R>(rb, Q, 0, c, wend, ib, n, Q, margin, B, best);
+                c = wend;
+            }
+        }
+    }
+    best = warp_min_u64(best);
+    if (lane == 0) S.wbest[warp] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = S.wbest[0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) m = S.wbest[w] < m ? S.wbest[w] : m;
+        S.key = m;
+    }
+    __syncthreads();
+    const unsigned long long k = S.key;
+    __syncthreads();
+    return k;
+}
 
 // Tiles per row block of the pair triangle (rows 1..n-3) for sweep(); one
 // thread of the CTA fills the table, callers synchronise afterwards.

@@ -31,6 +31,7 @@ template <int R, int NT, int TC>
 __global__ void __launch_bounds__(NT) serve_round_kernel(ServeArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ CtaShared<NT> S;
+    __shared__ CtaWindows W;
     OrderedCity* Q = reinterpret_cast<OrderedCity*>(smem_raw);
     uint32_t* route = reinterpret_cast<uint32_t*>(smem_raw + sizeof(OrderedCity) * A.max_n);
     uint32_t* bestr = route + A.max_n;
@@ -77,7 +78,9 @@ __global__ void __launch_bounds__(NT) serve_round_kernel(ServeArgs A) {
         uint64_t rng = st.rng;
         while (st.phase != kServeDone && spent < A.budget_pairs) {
             if (st.phase == kServeDescent) {
-                const unsigned long long key = sweep<R, NT, TC>(S, Q, n, st.margin);
+                window_stats_cta<NT>(W, Q, n);
+                __syncthreads();
+                const unsigned long long key = sweep_boxed<R, NT, TC>(S, W, Q, n, st.margin);
                 ++st.sweeps;
                 spent += pairs + n;  // + n: a sweep of a tiny tour still costs work
                 if (key == kNoMove) {

@@ -239,9 +239,7 @@ logo_status upload_route(logo_ctx* c, const uint32_t* route) {
     if (!route) return fail(c, LOGO_ERR_INVALID_ARG, "route is NULL");
     CK(c, cudaMemcpyAsync(c->d_route[0], route, sizeof(uint32_t) * c->n,
                           cudaMemcpyHostToDevice, c->stream));
-    CK(c, cudaMemsetAsync(c->d_seen, 0, sizeof(uint32_t) * ((c->n + 31) / 32), c->stream));
-    CK(c, cudaMemsetAsync(&c->d_st->bad_route, 0, sizeof(unsigned int), c->stream));
-    CK(c, cudaMemsetAsync(&c->d_st->cur, 0, sizeof(unsigned int), c->stream));
+    CK(c, launch_route_check_reset(bufs(c), c->stream));
     CK(c, launch_init_ordered(bufs(c), c->stream));
     c->have_route = true;
     return LOGO_OK;
@@ -289,8 +287,10 @@ bool use_coop(const logo_ctx* c) {
 logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
                         uint64_t* sweeps_out, bool reset = true) {
     if (max_moves == 0) max_moves = ~0ull >> 1;
-    if (reset) CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));
-    CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
+    if (reset)  // also clears the status word
+        CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));
+    else
+        CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
     // a fresh descent starts from zero moves and records its sweep count on
     // the device; a continued one needs the counters first
     uint64_t moves0 = 0, sweeps0 = 0;
@@ -607,8 +607,7 @@ logo_status logo_begin_descent(logo_ctx* c, uint64_t max_moves) {
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     if (max_moves == 0) max_moves = ~0ull >> 1;
-    CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));
-    CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
+    CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));  // clears status too
     return LOGO_OK;
 }
 
@@ -669,8 +668,7 @@ logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
     if (!c || !out) return LOGO_ERR_INVALID_ARG;
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
-    CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));
-    CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
+    CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));  // clears status too
     CK(c, launch_sweep(sweep_args(c), c->stream));
     logo_status s = read_state(c);
     if (s != LOGO_OK) return s;

@@ -89,6 +89,8 @@ cudaError_t launch_barrier_probe(CoopSync* cs, DevState* st, cudaStream_t s);
 // Builds Q[0] from xy and route[0] (route already uploaded to route[0]) and
 // checks that route[0] is a permutation of 0..n-1 (st->bad_route = 1 if not;
 // out-of-range entries are read as city 0).
+// Clears the seen bitmap, bad_route and cur; call before launch_init_ordered.
+cudaError_t launch_route_check_reset(const TourBufs& T, cudaStream_t s);
 cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s);
 // Prepares *st for a new descent: cur = 0 kept, counters cleared.
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,

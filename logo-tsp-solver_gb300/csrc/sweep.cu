@@ -24,6 +24,8 @@
 // ends up holding the lowest (delta, i, c), i.e. the reference CPU's choice
 // (i ascending, j ascending, strict <).  Keys reduce by warp shuffle, shared
 // memory, and one 64-bit atomicMin per CTA.
+#include <atomic>
+
 #include "logo_device.cuh"
 #include "logo_internal.h"
 #include "sweep_core.cuh"
@@ -869,14 +871,23 @@ static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool pre
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     attr_bytes(boxed_smem_bytes(kMaxBoxedCols, NW)));
     }
-    int device = 0, sms = 0, per_sm = 0;
+    // resident CTAs of this shape per device and tile width, computed once
+    static std::atomic<uint32_t> cached[64][kMaxBoxedCols / kWin7 + 1];
+    int device = 0;
     cudaError_t e = cudaGetDevice(&device);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_boxed_kernel<R, NW>,
-                                                          NW * 32, smem);
     if (e != cudaSuccess) return e;
-    const uint32_t resident = (uint32_t)(per_sm > 0 ? per_sm : 1) * (uint32_t)sms;
+    std::atomic<uint32_t>& slot = cached[(unsigned)device % 64][L.cb / kWin7];
+    uint32_t resident = slot.load(std::memory_order_relaxed);
+    if (resident == 0) {
+        int sms = 0, per_sm = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_boxed_kernel<R, NW>,
+                                                              NW * 32, smem);
+        if (e != cudaSuccess) return e;
+        resident = (uint32_t)(per_sm > 0 ? per_sm : 1) * (uint32_t)sms;
+        slot.store(resident, std::memory_order_relaxed);
+    }
     const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
     const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
     window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.n, L.wbox, L.wmax, L.rbox,

@@ -71,6 +71,7 @@ __global__ void init_ordered_kernel(const float2* __restrict__ xy,
 __global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves) {
     st->best_key = kNoMove;
     st->moves = 0;
+    st->status = 0u;
     st->converged = st->bad_route ? 1u : 0u;  // nothing to descend on a bad route
     st->sweeps_at_reset = st->sweeps;
     st->done_blocks = 0;
@@ -239,6 +240,26 @@ __global__ void save_best_kernel(TourBufs T) {
 }
 
 }  // namespace
+
+// Clears the permutation check before launch_init_ordered: the seen bitmap,
+// the bad-route flag and the current-buffer index (one launch instead of
+// three memsets per uploaded route).
+__global__ void route_check_reset_kernel(uint32_t* __restrict__ seen, uint32_t words,
+                                         DevState* st) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < words;
+         k += gridDim.x * blockDim.x)
+        seen[k] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->bad_route = 0u;
+        st->cur = 0u;
+    }
+}
+
+cudaError_t launch_route_check_reset(const TourBufs& T, cudaStream_t s) {
+    const uint32_t words = (T.n + 31) / 32;
+    route_check_reset_kernel<<<grid_for(words), kThreads, 0, s>>>(T.seen, words, T.st);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s) {
     init_ordered_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, T.route[0], T.Q[0], T.n,

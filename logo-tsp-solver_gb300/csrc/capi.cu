@@ -124,12 +124,12 @@ uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) /
 void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
     // measured on GB300 (one sweep: NN start tours of Gaussian mixtures, the
     // local optimum of the n = 100k one, uniform points on random tours): from
-    // n = 17.5k up the boxed screen is fastest (n = 100k NN tour: 0.090 ms with
+    // n = 17.5k up the boxed screen is fastest (n = 100k NN tour: 0.084 ms with
     // (4, 4, 128) tiles vs 0.61 local, 0.83 fused, 1.80 MUFU; at its local
-    // optimum 0.109 vs 0.68; random tour 0.39 vs 0.68, 0.23 with (8, 8, 1024)
-    // tiles; n = 40k: 0.063 ms with 64-column tiles vs 0.078 with 128 and
+    // optimum 0.102 vs 0.68; random tour 0.39 vs 0.68, 0.23 with (8, 8, 1024)
+    // tiles; n = 40k: 0.063 ms with 64-column tiles vs 0.073 with 128 and
     // 0.149 local; n = 20k: 0.067 vs 0.067 local and 0.084 MUFU; n = 1M random
-    // tour: 7.1 ms with (8, 8, 1024) vs 54.8 local); below it the MUFU screen,
+    // tour: 6.0 ms with (8, 8, 1024) vs 54.8 local); below it the MUFU screen,
     // whose test is tighter on short tours, wins, with 64-column tiles from 3k
     // (n = 10k: 0.030 ms vs 0.063 boxed and 0.042 with (4, 4, 128) MUFU tiles).
     variant = LOGO_SWEEP_MUFU;

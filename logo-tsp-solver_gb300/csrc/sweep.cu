@@ -576,6 +576,8 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
     BoxedSlot* slot = reinterpret_cast<BoxedSlot*>(smem_raw + 16);  // 48 bytes
     OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + kBoxedStageOffset);
     uint32_t* queue = reinterpret_cast<uint32_t*>(smem_raw + boxed_queue_offset(cb));
+    __shared__ float4 sbox[kWin7];  // the claimed tile's window statistics
+    __shared__ float smax[kWin7];
     float* cx = reinterpret_cast<float*>(smem_raw + boxed_cx_offset(cb, NW));
     float* cy = cx + sweep6_cols4(cb);
     float* cc = cy + sweep6_cols4(cb);
@@ -624,6 +626,13 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
         const float4* tbox = gbox + (col0 - 3) / kWin7;
         const float* tmax = gmax + (col0 - 3) / kWin7;
         const uint32_t ib = row0 + threadIdx.x * R;
+        // the tile's window statistics, all loaded at once (loading them
+        // inside the window loop cost one round trip each)
+        if (threadIdx.x < kWin7 && ((item.z >> threadIdx.x) & 1u)) {
+            sbox[threadIdx.x] = tbox[threadIdx.x];
+            smax[threadIdx.x] = tmax[threadIdx.x];
+        }
+        __syncthreads();
         uint32_t open = 0;  // windows in which some row of this thread is open
         uint32_t rows = 0;  // open rows over this thread's units
         if (ib + 3 <= n) {
@@ -632,7 +641,7 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
             for (uint32_t m = item.z; m; m &= m - 1) {
                 const uint32_t w = __ffs(m) - 1;
                 if (col0 + (w + 1) * kWin7 <= ib + 2) continue;  // left of the first pair
-                const uint32_t rm = rows_open7<R>(rb, __ldg(tbox + w), __ldg(tmax + w));
+                const uint32_t rm = rows_open7<R>(rb, sbox[w], smax[w]);
                 if (rm) {
                     queue[atomicAdd(&slot->units, 1u)] = (threadIdx.x << 24) | (w << 16) | rm;
                     open |= 1u << w;

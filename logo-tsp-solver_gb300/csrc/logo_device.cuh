@@ -3,16 +3,19 @@
 // Distances.  The reference's per-edge distance is
 //     (int)(sqrtf(dx*dx + dy*dy) + 0.5f)          src/cuda/cuda_common.h:33-40
 // Its kernels are built with --use_fast_math (Makefile:84), its CPU length
-// with the C compiler's default contraction; this build fixes the arithmetic
-// to IEEE binary32 with no FMA contraction and a correctly rounded square
-// root, so the CPU oracle and the device agree bit for bit (exact_dist).
+// with the C compiler's default contraction; this library fixes the
+// arithmetic to IEEE binary32 with no FMA contraction and a correctly rounded
+// square root, so the CPU oracle and the device agree bit for bit
+// (exact_dist).
 //
-// The sweep does not evaluate exact_dist for every pair.  It evaluates
-// approx_dist (one MUFU sqrt) for every pair and a conservative error bound
-// M (host-side filter_margin) tells it which pairs could still tie or beat
-// the best exact delta it has seen; only those are re-evaluated exactly.  A
-// pair whose exact delta is <= the bound always passes the filter, so the
-// chosen move is the exact lowest-(delta, i, j) one.
+// The sweeps do not evaluate exact_dist for every pair.  The MUFU screen
+// evaluates approx_dist (one MUFU sqrt) for every pair and a conservative
+// error bound M (host-side filter_margin) tells it which pairs could still
+// tie or beat the best exact delta it has seen; only those are re-evaluated
+// exactly (the other screens use proven bounds on squared distances and
+// bounding boxes instead of M).  A pair whose exact delta is <= the bound
+// always passes the filter, so the chosen move is the exact lowest-(delta,
+// i, j) one.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>

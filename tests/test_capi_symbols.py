@@ -54,3 +54,6 @@ def test_version_and_error_path_without_compute(lg):
     assert b"NULL" in L.logo_last_error(None)
     assert L.logo_best_move(None, None, None) == 1
     assert L.logo_ctx_destroy(None) == 0
+    assert L.logo_ctx_set_kernel(None, lg.SWEEP_BOXED, 4, 4, 128) == 1
+    assert L.logo_ctx_set_descent_mode(None, lg.DESCENT_GRAPH) == 1
+    assert L.logo_diag_wait_limits(0, None, None, None) == 1

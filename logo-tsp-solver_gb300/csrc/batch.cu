@@ -30,6 +30,9 @@
 
 namespace logo {
 
+static_assert((kBatchMaxN - 3 + kWin7 - 1) / kWin7 <= kCtaWindows,
+              "the CTA sweep's window statistics cover the largest instance");
+
 namespace {
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned int* p) {

@@ -300,6 +300,11 @@ def run_ours(a, world, rank, local, dist):
                        "(MEASURED_PEAKS.json)",
         "achieved_pairs_per_s": achieved_pairs,
         "sweep_ms_mean": round(statistics.mean(sweep_ms), 4),
+        "note": "achieved counts every pair of the sweep as decided; the screens decide "
+                "most pairs without per-pair arithmetic (the boxed screen closes whole "
+                "rows x 32-column blocks by a bounding-box test), always returning the "
+                "reference's move, so frac above 1 measures pruning, not lane throughput; "
+                "thread instructions per pair and issue-slot use are in profiles/",
     }
     if clocks.get("sm_mhz"):
         roof["frac_at_sampled_clock"] = round(

@@ -127,7 +127,7 @@ __device__ __forceinline__ unsigned long long sweep(CtaShared<NT>& S, const Orde
     constexpr uint32_t RT = 32 * R;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t best = kNoMove;
-    if (n >= 5) {
+    if (n >= 4) {
         const uint32_t nrb = (n - 3 + RT - 1) / RT;  // row blocks over rows 1..n-3
         const uint32_t total = S.tiles_before[nrb];
         uint32_t rbk = 0;
@@ -211,7 +211,7 @@ __device__ __forceinline__ unsigned long long sweep_boxed(CtaShared<NT>& S, cons
     constexpr uint32_t RT = 32 * R;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t best = kNoMove;
-    if (n >= 5) {
+    if (n >= 4) {
         const uint32_t nrb = (n - 3 + RT - 1) / RT;  // row blocks over rows 1..n-3
         const uint32_t total = S.tiles_before[nrb];
         uint32_t rbk = 0;
@@ -268,7 +268,7 @@ __device__ __forceinline__ void fill_tile_table(SharedT& S, uint32_t n) {
     constexpr uint32_t RT = 32 * R;
     uint32_t acc = 0, rbk = 0;
     S.tiles_before[0] = 0;
-    if (n >= 5) {
+    if (n >= 4) {
         for (uint32_t row0 = 1; row0 + 3 <= n; row0 += RT, ++rbk) {
             acc += (n - row0 - 2 + TC - 1) / TC;
             S.tiles_before[rbk + 1] = acc;

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(NT) serve_round_kernel(ServeArgs A) {
             st.best_len = st.start_len;
             st.phase = kServeDescent;
         }
-        const unsigned long long pairs = n >= 5 ? (unsigned long long)(n - 2) * (n - 3) / 2 : 0;
+        const unsigned long long pairs = n >= 4 ? (unsigned long long)(n - 2) * (n - 3) / 2 : 0;
         const unsigned long long move_cap = 64ull * n * n + 1024;
         unsigned long long spent = 0;
         uint64_t rng = st.rng;

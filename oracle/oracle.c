@@ -94,7 +94,7 @@ static uint64_t sweep_rows(const ordered_t *o, uint32_t lo, uint32_t hi,
     const int32_t *E = o->e;
     uint64_t best = UINT64_MAX;
     int32_t bestd = 0;
-    if (n < 5)
+    if (n < 4)
         return best;
     if (hi > n - 2)
         hi = n - 2;
@@ -222,16 +222,29 @@ static void *mt_worker(void *p)
     return NULL;
 }
 
+static uint64_t sweep_ordered_mt(const ordered_t *o, uint32_t row_lo, uint32_t row_hi,
+                                 int threads);
+
 uint64_t lo_best_move_mt(const float *xy, const uint32_t *route, uint32_t n,
                          uint32_t row_lo, uint32_t row_hi, int threads)
 {
     ordered_t o;
-    if (threads < 1)
-        threads = 1;
     if (ordered_init(&o, xy, route, n)) {
         ordered_free(&o);
         return UINT64_MAX;
     }
+    uint64_t best = sweep_ordered_mt(&o, row_lo, row_hi, threads);
+    ordered_free(&o);
+    return best;
+}
+
+/* Rows [row_lo, row_hi) of an ordered tour on `threads` pthreads. */
+static uint64_t sweep_ordered_mt(const ordered_t *o, uint32_t row_lo, uint32_t row_hi,
+                                 int threads)
+{
+    const uint32_t n = o->n;
+    if (threads < 1)
+        threads = 1;
     if (row_lo < 1)
         row_lo = 1;
     if (row_hi == 0 || row_hi > n)
@@ -242,7 +255,7 @@ uint64_t lo_best_move_mt(const float *xy, const uint32_t *route, uint32_t n,
     mt_arg_t *args = (mt_arg_t *)malloc(sizeof(mt_arg_t) * threads);
     uint32_t block = 32;
     for (int t = 0; t < threads; t++) {
-        args[t].o = &o;
+        args[t].o = o;
         args[t].lo = row_lo;
         args[t].hi = row_hi;
         args[t].block = block;
@@ -259,7 +272,6 @@ uint64_t lo_best_move_mt(const float *xy, const uint32_t *route, uint32_t n,
     }
     free(th);
     free(args);
-    ordered_free(&o);
     return best;
 }
 
@@ -318,9 +330,11 @@ uint64_t lo_tour_length(const float *xy, const uint32_t *route, uint32_t n)
     return d;
 }
 
-/* src/solvers/twoOptLocalSolver.cpp:22-64 */
-int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
-                   uint64_t max_moves, int32_t *move_log, uint64_t log_cap)
+/* src/solvers/twoOptLocalSolver.cpp:22-64; each sweep on `threads` pthreads
+ * (the same move: the parallel sweep keeps the lowest-(delta, i, j) rule). */
+static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
+                            uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
+                            int threads)
 {
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
     int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(n + 1));
@@ -337,8 +351,9 @@ int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
         }
         for (uint32_t k = 1; k < n; k++)
             o.e[k] = lo_dist(o.x[k - 1], o.y[k - 1], o.x[k], o.y[k]);
-        uint64_t key = sweep_rows(&o, 1, n, buf, buf + (n + 1),
-                                  buf + 2 * (n + 1));
+        uint64_t key = threads > 1 ? sweep_ordered_mt(&o, 1, n, threads)
+                                   : sweep_rows(&o, 1, n, buf, buf + (n + 1),
+                                                buf + 2 * (n + 1));
         if (key == UINT64_MAX)
             break;
         if ((uint64_t)moves >= max_moves) {
@@ -362,6 +377,19 @@ int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
     free(tmp);
     free(buf);
     return moves;
+}
+
+int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
+                   uint64_t max_moves, int32_t *move_log, uint64_t log_cap)
+{
+    return descend_impl(xy, route, n, max_moves, move_log, log_cap, 1);
+}
+
+int64_t lo_descend_mt(const float *xy, uint32_t *route, uint32_t n,
+                      uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
+                      int threads)
+{
+    return descend_impl(xy, route, n, max_moves, move_log, log_cap, threads);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -404,9 +432,9 @@ void lo_kick_double_bridge(uint32_t *route, uint32_t n, uint64_t *rng,
 /* src/solvers/ILSGlobalSolverSequential.cpp:60-100, stop rule replaced by an
  * explicit kick count (the reference's stop test needs a known optimum,
  * :98-99, and ends after one pass otherwise). */
-int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
-           uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
-           lo_ils_stats *stats)
+static int ils_impl(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
+                    uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
+                    lo_ils_stats *stats, int threads)
 {
     uint32_t *best = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
@@ -418,7 +446,7 @@ int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
     uint64_t best_len = st.start_length;
     memcpy(best, route, sizeof(uint32_t) * n);
     for (uint32_t it = 0;; it++) {
-        int64_t m = lo_descend(xy, route, n, max_moves_per_descent, NULL, 0);
+        int64_t m = descend_impl(xy, route, n, max_moves_per_descent, NULL, 0, threads);
         st.descents++;
         if (m < 0) {
             rc = -1;
@@ -447,6 +475,21 @@ int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
     free(best);
     free(tmp);
     return rc;
+}
+
+int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
+           uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
+           lo_ils_stats *stats)
+{
+    return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats, 1);
+}
+
+int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
+              uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
+              lo_ils_stats *stats, int threads)
+{
+    return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats,
+                    threads);
 }
 
 /* ------------------------------------------------------------------------ */

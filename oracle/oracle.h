@@ -84,6 +84,10 @@ uint64_t lo_tour_length(const float *xy, const uint32_t *route, uint32_t n);
  * log_cap moves.  Returns the number of moves, or -1 if max_moves was hit. */
 int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
                    uint64_t max_moves, int32_t *move_log, uint64_t log_cap);
+/* The same descent with every sweep split over `threads` pthreads (same moves). */
+int64_t lo_descend_mt(const float *xy, uint32_t *route, uint32_t n,
+                      uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
+                      int threads);
 
 /* Kick kinds for the ILS perturbation. */
 #define LO_KICK_SEGMENT 0       /* reference kick, ILSGlobalSolver.cpp:37-48 */
@@ -116,6 +120,10 @@ typedef struct {
 int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
            uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
            lo_ils_stats *stats);
+/* The same ILS with every sweep split over `threads` pthreads (same result). */
+int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
+              uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
+              lo_ils_stats *stats, int threads);
 
 /* Nearest-neighbour start tour, initRoute_KD_NN
  * (src/utils/kdtree_utils.c:279-301): start at city 0, repeatedly go to the

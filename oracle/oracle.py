@@ -65,6 +65,13 @@ def lib():
         L.lo_descend.restype = ctypes.c_int64
         L.lo_descend.argtypes = [_f32p, _u32p, ctypes.c_uint32, ctypes.c_uint64,
                                  _i32p, ctypes.c_uint64]
+        L.lo_descend_mt.restype = ctypes.c_int64
+        L.lo_descend_mt.argtypes = [_f32p, _u32p, ctypes.c_uint32, ctypes.c_uint64,
+                                    _i32p, ctypes.c_uint64, ctypes.c_int]
+        L.lo_ils_mt.restype = ctypes.c_int
+        L.lo_ils_mt.argtypes = [_f32p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
+                                ctypes.POINTER(IlsStats), ctypes.c_int]
         L.lo_kick_segment.restype = None
         L.lo_kick_segment.argtypes = [_u32p, ctypes.c_uint32, _u64p, _u32p]
         L.lo_kick_double_bridge.restype = None
@@ -144,16 +151,17 @@ def tour_length(xy, route):
     return lib().lo_tour_length(pxy, pr, len(route))
 
 
-def descend(xy, route, max_moves=None, log_cap=0):
-    """Returns (final_route, moves, log) where log is an (m, 3) int32 array."""
+def descend(xy, route, max_moves=None, log_cap=0, threads=1):
+    """Returns (final_route, moves, log) where log is an (m, 3) int32 array.
+    threads > 1 splits every sweep over that many host threads (same moves)."""
     xy, pxy = _f32(xy)
     r = np.array(route, dtype=np.uint32, copy=True)
     n = len(r)
     if max_moves is None:
         max_moves = 64 * n * n + 1024
     log = np.zeros((max(log_cap, 1), 3), dtype=np.int32)
-    m = lib().lo_descend(pxy, r.ctypes.data_as(_u32p), n, max_moves,
-                         log.ctypes.data_as(_i32p), log_cap)
+    m = lib().lo_descend_mt(pxy, r.ctypes.data_as(_u32p), n, max_moves,
+                            log.ctypes.data_as(_i32p), log_cap, max(1, int(threads)))
     if m < 0:
         raise RuntimeError("oracle descent exceeded max_moves")
     return r, m, log[: min(m, log_cap)]
@@ -169,15 +177,15 @@ def kick(route, rng_state, kind=KICK_SEGMENT):
     return r, st.value
 
 
-def ils(xy, route, kicks, seed, kind=KICK_SEGMENT, max_moves=None):
+def ils(xy, route, kicks, seed, kind=KICK_SEGMENT, max_moves=None, threads=1):
     xy, pxy = _f32(xy)
     r = np.array(route, dtype=np.uint32, copy=True)
     n = len(r)
     if max_moves is None:
         max_moves = 64 * n * n + 1024
     st = IlsStats()
-    rc = lib().lo_ils(pxy, r.ctypes.data_as(_u32p), n, kicks, seed, kind, max_moves,
-                      ctypes.byref(st))
+    rc = lib().lo_ils_mt(pxy, r.ctypes.data_as(_u32p), n, kicks, seed, kind, max_moves,
+                         ctypes.byref(st), max(1, int(threads)))
     if rc:
         raise RuntimeError("oracle ILS descent exceeded max_moves")
     return r, {k: getattr(st, k) for k, _ in IlsStats._fields_}

@@ -62,6 +62,35 @@ def steps():
             "hash": np.array(hashes)}
 
 
+def small_n():
+    """Tours of 4 to 7 cities: single steps and whole descents.  At n = 4 the
+    reference's loop (src/solvers/cpuSolver.cpp:104,123: i < n-2, j < n-1)
+    evaluates exactly one pair, (i, j) = (1, 2), reported as (1, 3)."""
+    rows, outs, hashes, logs, fin = [], [], [], [], []
+    square = np.array([[0, 0], [10, 0], [10, 10], [0, 10]], dtype=np.float32)
+    cases = [("square", square, np.array([0, 2, 1, 3], dtype=np.uint32), -1, -1)]
+    for n in (4, 5, 6, 7):
+        for gi, gen in enumerate(GENS):
+            for s in range(8):
+                seed = 7000 * n + 10 * gi + s
+                cases.append((gen, make_instance(gen, n, seed),
+                              instances.random_tour(n, seed + 1), seed, gi))
+    for gen, xy, r, seed, gi in cases:
+        n = len(r)
+        outs.append(ref.step(xy, r))
+        fr, m, log, length = ref.descend(xy, r)
+        logs.append(log)
+        rows.append((gi, n, seed, seed + 1, m, length))
+        hashes.append(digest(xy, r))
+        fin.append(fr)
+    off = np.cumsum([0] + [len(x) for x in logs]).astype(np.int64)
+    foff = np.cumsum([0] + [len(x) for x in fin]).astype(np.int64)
+    return {"spec": np.array(rows, dtype=np.int64), "out": np.array(outs, dtype=np.int32),
+            "hash": np.array(hashes), "log": np.concatenate(logs).reshape(-1, 3).astype(np.int32),
+            "log_offsets": off, "final": np.concatenate(fin).astype(np.uint32),
+            "final_offsets": foff}
+
+
 def descents():
     logs, meta, hashes, fin = [], [], [], []
     for seed in range(1, 17):
@@ -166,6 +195,11 @@ def main():
         np.savez_compressed(os.path.join(HERE, "mf_tours.npz"), **mf_tours(a.ref))
         print("mf_tours.npz written to", HERE)
         return
+    if a.only == "small_n":
+        np.savez_compressed(os.path.join(HERE, "small_n.npz"), **small_n())
+        print("small_n.npz written to", HERE)
+        return
+    np.savez_compressed(os.path.join(HERE, "small_n.npz"), **small_n())
     np.savez_compressed(os.path.join(HERE, "mf_tours.npz"), **mf_tours(a.ref))
     np.savez_compressed(os.path.join(HERE, "steps.npz"), **steps())
     np.savez_compressed(os.path.join(HERE, "descents_n1000.npz"), **descents())

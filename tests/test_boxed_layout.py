@@ -12,7 +12,7 @@ WIN = 32
 def make_tiles(n, rt, cb):
     # the host tile list: rows [row0, row0 + rt), columns [col0, col0 + cb)
     out = []
-    if n < 5:
+    if n < 4:
         return out
     row0 = 1
     while row0 + 3 <= n:

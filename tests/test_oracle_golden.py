@@ -109,3 +109,23 @@ def test_tsplib_fixtures(oracle_mod, name):
         final_len, start_len = (int(v) for v in g[name + "_len"])
         assert oracle_mod.tour_length(xy, fr) == final_len
         assert oracle_mod.tour_length(xy, nn) == start_len
+
+
+def test_small_tours(oracle_mod, inst):
+    """Tours of 4 to 7 cities (small_n.npz): the single step and the whole
+    descent; at n = 4 the reference evaluates its one pair (1, 2) -> (1, 3)."""
+    g = load("small_n.npz")
+    square = np.array([[0, 0], [10, 0], [10, 10], [0, 10]], dtype=np.float32)
+    for k, (gi, n, seed, rseed, m, length) in enumerate(g["spec"]):
+        if gi < 0:
+            xy, r = square, np.array([0, 2, 1, 3], dtype=np.uint32)
+        else:
+            xy = make_instance(inst, GENS[gi], int(n), int(seed))
+            r = inst.random_tour(int(n), int(rseed))
+        assert digest(xy, r) == g["hash"][k]
+        assert oracle_mod.best_move(xy, r) == tuple(int(v) for v in g["out"][k]), (n, seed)
+        fr, mo, log = oracle_mod.descend(xy, r, log_cap=1 << 10)
+        assert mo == m and oracle_mod.tour_length(xy, fr) == length
+        assert np.array_equal(log, g["log"][g["log_offsets"][k]:g["log_offsets"][k + 1]])
+        assert np.array_equal(fr, g["final"][g["final_offsets"][k]:g["final_offsets"][k + 1]])
+    assert (g["spec"][:, 1] == 4).sum() >= 20

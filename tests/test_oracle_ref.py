@@ -24,6 +24,18 @@ def test_step_and_descent(oracle_mod, inst, seed):
     assert ref.length(xy, r) == oracle_mod.tour_length(xy, r)
 
 
+def test_tours_of_four_to_six_cities(oracle_mod, inst):
+    """The reference's loop bounds (i < n-2, j < n-1) leave one pair at n = 4."""
+    for seed in range(12):
+        for n in (4, 5, 6):
+            xy = inst.uniform_int(n, seed)
+            r = inst.random_tour(n, seed + 7)
+            assert oracle_mod.best_move(xy, r) == ref.step(xy, r), (n, seed)
+            fr, m, log, length = ref.descend(xy, r)
+            fo, mo, logo = oracle_mod.descend(xy, r, log_cap=64)
+            assert m == mo and np.array_equal(fr, fo) and np.array_equal(log, logo)
+
+
 def test_duplicate_points_and_ties(oracle_mod, inst):
     rng = np.random.default_rng(1)
     xy = np.floor(rng.random((120, 2)) * 8).astype(np.float32)

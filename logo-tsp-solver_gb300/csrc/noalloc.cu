@@ -16,7 +16,16 @@
 // the library and stays allocated until the process exits.  Host code cannot
 // use the array's name as a device address, so the first call on each device
 // looks the address up with cudaGetSymbolAddress (with that device current)
-// and caches it; make that first call before any stream capture.
+// and caches it; make that first call before any stream capture.  The cache
+// is keyed by the device's current context (its driver-assigned unique id),
+// so a call after cudaDeviceReset, which re-creates the primary context and
+// with it the array, looks the address up again instead of using the old
+// one.
+//
+// The coordinates are read as 8-byte (x, y) pairs, so coords must be 8-byte
+// aligned (any cudaMalloc'd array and any even element offset into one);
+// route, out and status_out must be 4-byte aligned.  Misaligned pointers are
+// refused on the host with LOGO_ERR_INVALID_ARG before any work is enqueued.
 //
 // Every call shares the array and the array keeps the previous call's
 // contents: each call clears the key, bounding box and status first.  Calls
@@ -26,6 +35,8 @@
 #include <cmath>
 #include <cstdint>
 #include <mutex>
+
+#include <cudaTypedefs.h>
 
 #include "../../include/logo_gpu.h"
 #include "logo_device.cuh"
@@ -176,8 +187,43 @@ __global__ void noalloc_finish(const unsigned char* scratch, logo_move* out, int
     if (status_out) *status_out = (int32_t)h->status;
 }
 
+// The scratch array's device address per device, with the id of the context
+// it was looked up in (0: not looked up yet).
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    void* ptr;
+};
 std::mutex g_mu;
-void* g_scratch[64] = {nullptr};
+ScratchAddr g_scratch[64] = {};
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+PFN_cuCtxGetId_v12000 g_ctx_id = nullptr;
+bool g_ctx_fns_tried = false;
+
+// Unique id of the calling thread's current context; 0 if the driver cannot
+// tell, in which case the address is looked up on every call.
+unsigned long long current_ctx_id() {
+    if (!g_ctx_fns_tried) {
+        g_ctx_fns_tried = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault,
+                                             &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault,
+                                             &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            g_ctx_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f1);
+            g_ctx_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f2);
+        }
+    }
+    if (!g_ctx_current || !g_ctx_id) return 0ull;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0ull;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return 0ull;
+    if (g_ctx_id(ctx, &id) != CUDA_SUCCESS) return 0ull;
+    return id;
+}
 
 }  // namespace
 
@@ -186,19 +232,25 @@ extern "C" logo_status logo_best_move_noalloc(const logo_xy* coords, const uint3
                                               void* stream) {
     if (!coords || !route || !out) return LOGO_ERR_INVALID_ARG;
     if (n < 3 || n > kNoAllocMax) return LOGO_ERR_INVALID_ARG;
+    if ((reinterpret_cast<uintptr_t>(coords) & 7u) || (reinterpret_cast<uintptr_t>(route) & 3u) ||
+        (reinterpret_cast<uintptr_t>(out) & 3u) || (reinterpret_cast<uintptr_t>(status_out) & 3u))
+        return LOGO_ERR_INVALID_ARG;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return LOGO_ERR_NO_DEVICE;
     if (dev >= 64) return LOGO_ERR_INVALID_ARG;
     void* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch[dev]) {
+        const unsigned long long id = current_ctx_id();
+        ScratchAddr& a = g_scratch[dev];
+        if (!a.ptr || id == 0ull || a.ctx_id != id) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, logo_noalloc_scratch) != cudaSuccess || !p)
                 return LOGO_ERR_CUDA;
-            g_scratch[dev] = p;
+            a.ptr = p;
+            a.ctx_id = id;
         }
-        scratch = g_scratch[dev];
+        scratch = a.ptr;
     }
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char* sc = static_cast<unsigned char*>(scratch);
@@ -206,7 +258,7 @@ extern "C" logo_status logo_best_move_noalloc(const logo_xy* coords, const uint3
     const unsigned prep_grid = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
     noalloc_prepare<<<prep_grid, 256, 0, s>>>(reinterpret_cast<const float2*>(coords), route, n,
                                               sc);
-    if (n >= 5) {
+    if (n >= 4) {
         const dim3 grid((n - 3 + kColsPerCta - 1) / kColsPerCta,
                         (n - 3 + kRowsPerCta - 1) / kRowsPerCta);
         noalloc_sweep<<<grid, kNW * 32, 0, s>>>(n, sc);

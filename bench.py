@@ -162,9 +162,6 @@ def measured_peaks():
 
 # sweep kernel per LOGO_SWEEP_* variant: (kernel, screen)
 SWEEP_KERNELS = {0: ("sweep_kernel", "MUFU screen"),
-                 1: ("sweep_kernel2", "packed MUFU screen"),
-                 2: ("sweep_kernel3", "square-root-free screen"),
-                 3: ("sweep_kernel4", "packed square-root-free screen"),
                  4: ("sweep_kernel5", "fused two-stage square-root-free screen"),
                  5: ("sweep_kernel6", "local-coordinate expanded screen"),
                  6: ("sweep_boxed_kernel", "boxed screen: row-block and window bounding "

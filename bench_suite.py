@@ -1,10 +1,10 @@
 """Benchmarks of the workloads beside bench.py's headline (one JSON line each).
 
-  python logo-tsp-solver_gb300/bench_suite.py plain    # n=1000 integer coords, descent
-  python logo-tsp-solver_gb300/bench_suite.py sweep    # one sweep at n=10k, 100k, 1M
-  python logo-tsp-solver_gb300/bench_suite.py large    # n=100k NN descent + 1000 kicks
-  python logo-tsp-solver_gb300/bench_suite.py serve    # Poisson request stream
-  python logo-tsp-solver_gb300/bench_suite.py construct  # start tours, host vs device
+  python bench_suite.py plain    # n=1000 integer coords, descent
+  python bench_suite.py sweep    # one sweep at n=10k, 100k, 1M
+  python bench_suite.py large    # n=100k NN descent + 1000 kicks
+  python bench_suite.py serve    # Poisson request stream
+  python bench_suite.py construct  # start tours, host vs device
 
 All inputs are seeded synthetic instances (instances.py).  The oracle (CPU
 restatement of the reference) is used only where a line reports a CPU
@@ -19,9 +19,8 @@ import time
 
 import numpy as np
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-ROOT = os.path.dirname(HERE)
-sys.path.insert(0, HERE)
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "logo-tsp-solver_gb300"))
 
 import instances  # noqa: E402
 import logo_gpu as lg  # noqa: E402

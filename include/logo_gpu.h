@@ -148,12 +148,16 @@ logo_status logo_descend_trace(logo_ctx *ctx, uint32_t *route_inout, uint64_t ma
  * (optional; receives LOGO_OK, or LOGO_ERR_INVALID_ARG when route is not a
  * permutation of 0..n-1 or the coordinates are unusable).  Work is enqueued
  * on `stream` (a cudaStream_t; NULL = legacy default stream) and the call
- * returns without waiting.  It allocates nothing: its working memory is a
+ * returns without waiting.  coords must be 8-byte aligned (it is read as
+ * (x, y) pairs: a cudaMalloc'd array, or an even element offset into one);
+ * route, out and status_out 4-byte aligned; misaligned pointers are refused
+ * with LOGO_ERR_INVALID_ARG before any work.  It allocates nothing: its working memory is a
  * fixed static device array of LOGO_NOALLOC_MAX_CITIES cities (1 MiB plus an
  * 8.25 KiB header) that every GPU loading the library holds until exit.
  * n above that maximum is rejected with LOGO_ERR_INVALID_ARG.  The first call
  * on each device looks up the array's device address (make it before any
- * stream capture).  All calls share the array, so calls whose work overlaps
+ * stream capture; a device reset re-creates the array, and the first call
+ * after it looks the address up again).  All calls share the array, so calls whose work overlaps
  * on the GPU race with each other; the caller must order them. */
 logo_status logo_best_move_noalloc(const logo_xy *coords, const uint32_t *route, uint32_t n,
                                    logo_move *out, int32_t *status_out, void *stream);
@@ -459,11 +463,8 @@ logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
  * n, see logo_ctx_info.variant).
  * LOGO_SWEEP_MUFU: pairs are screened with approximate square roots (MUFU)
  *   and an error margin.
- * LOGO_SWEEP_MUFU_PACKED: the same, issued as paired f32x2 arithmetic.
- * LOGO_SWEEP_SQUARED: screened with squared distances against
- *   (B + e_i + e_c + 5)^2, no square root on the fast path.
- * LOGO_SWEEP_SQUARED_PACKED: the squared screen with f32x2 distances and a
- *   per-row threshold over 32-column windows.
+ * Values 1-3 are retired (a paired-f32x2 MUFU screen and two plain
+ *   squared-distance screens that no size chose; LOGO_ERR_INVALID_ARG).
  * LOGO_SWEEP_FUSED: two-stage squared screen with the window threshold
  *   folded into the sum of squares: d(i, c) for every pair (FADD2/FFMA2, two
  *   rows at a time), d(i-1, c-1) only where that passes; threads share the
@@ -481,17 +482,12 @@ logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
  *   (or, on tiles where most rows are open, with the local screen).  Tile
  *   widths must be multiples of 32 up to 1024. */
 #define LOGO_SWEEP_MUFU 0
-#define LOGO_SWEEP_MUFU_PACKED 1
-#define LOGO_SWEEP_SQUARED 2
-#define LOGO_SWEEP_SQUARED_PACKED 3
 #define LOGO_SWEEP_FUSED 4
 #define LOGO_SWEEP_LOCAL 5
 #define LOGO_SWEEP_BOXED 6
 /* Selects variant and tile shape together (logo_ctx_set_shape keeps the
- * variant).  Shapes per variant: SQUARED (R,NW) in {(2,2),(4,2),(4,4),(8,4),
- * (8,8),(16,4)}; MUFU {(2,2),(2,4),(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)};
- * MUFU_PACKED {(4,2),(4,4),(8,4),(8,8),(16,2),(16,4)}; SQUARED_PACKED
- * {(4,4),(8,4),(8,8),(16,4)}; FUSED {(4,2),(4,4),(4,8),(8,2),(8,4),(8,8),(16,4)};
+ * variant).  Shapes per variant: MUFU (R,NW) in {(2,2),(2,4),(4,2),(4,4),
+ * (4,8),(8,4),(8,8),(16,4)}; FUSED {(4,2),(4,4),(4,8),(8,2),(8,4),(8,8),(16,4)};
  * LOCAL and BOXED {(4,2),(4,4),(4,8),(8,4),(8,8),(16,4)}; 16 <= cols <= 4096
  * (BOXED: a multiple of 32, at most 1024). */
 logo_status logo_ctx_set_kernel(logo_ctx *ctx, int variant, int rows_per_thread,

@@ -47,7 +47,7 @@ struct logo_ctx {
     uint32_t ntiles = 0;
     int R = 8, NW = 4;
     uint32_t cb = 1024;
-    int variant = LOGO_SWEEP_SQUARED;
+    int variant = LOGO_SWEEP_MUFU;
     float margin = 0.f;
     double diag = 0.0;
     cudaGraphExec_t chunk_exec = nullptr;
@@ -117,7 +117,7 @@ SweepLaunch sweep_args(const logo_ctx* c) {
     return L;
 }
 
-uint64_t pairs_of(uint32_t n) { return n < 5 ? 0 : (uint64_t)(n - 2) * (n - 3) / 2; }
+uint64_t pairs_of(uint32_t n) { return n < 4 ? 0 : (uint64_t)(n - 2) * (n - 3) / 2; }
 
 // Default tile shape by size (overridable through logo_ctx_set_shape and
 // logo_ctx_set_kernel).
@@ -156,7 +156,7 @@ void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
 // [col0, col0 + cb); full tiles first, diagonal tiles last.
 std::vector<uint2> make_tiles(uint32_t n, int R, int NW, uint32_t cb) {
     std::vector<uint2> full, diag;
-    if (n < 5) return full;
+    if (n < 4) return full;
     const uint32_t rt = (uint32_t)(NW * 32 * R);
     for (uint32_t row0 = 1; row0 + 3 <= n; row0 += rt) {
         const uint32_t row_last = std::min(row0 + rt - 1, n - 3);
@@ -580,8 +580,9 @@ logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
 
 logo_status logo_ctx_set_kernel(logo_ctx* c, int variant, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
-    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_BOXED)
-        return fail(c, LOGO_ERR_INVALID_ARG, "unknown sweep variant");
+    if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_BOXED ||
+        (variant > LOGO_SWEEP_MUFU && variant < LOGO_SWEEP_FUSED))
+        return fail(c, LOGO_ERR_INVALID_ARG, "unknown or retired sweep variant");
     if (!sweep_shape_supported(R, NW, variant) || cb < 16 || cb > 4096 ||
         !sweep_cols_supported(variant, cb))
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape for this variant");

@@ -29,9 +29,7 @@
 #include "logo_device.cuh"
 #include "logo_internal.h"
 #include "sweep_core.cuh"
-#include "sweep_core2.cuh"
 #include "sweep_core3.cuh"
-#include "sweep_core4.cuh"
 #include "sweep_core5.cuh"
 #include "sweep_core6.cuh"
 #include "sweep_core7.cuh"
@@ -80,134 +78,6 @@ __global__ void __launch_bounds__(NW * 32)
     refresh_thresholds<R>(rb, Q, ib, n, B, margin);
     if (mbar_wait_bounded(bar, 0, &st->status))
         walk_columns<R>(rb, cols, col0 - 1, col0, col_end, ib, n, Q, margin, B, best);
-
-    best = warp_min_u64(best);
-    if (lane == 0) wbest[warp] = best;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t m = wbest[0];
-#pragma unroll
-        for (int w = 1; w < NW; ++w) m = wbest[w] < m ? wbest[w] : m;
-        if (m != kNoMove) atomicMin(&st->best_key, (unsigned long long)m);
-    }
-}
-
-// Square-root-free variant (sweep_core3.cuh): same tiling and staging as
-// sweep_kernel; the fast path needs no MUFU operation.
-template <int R, int NW>
-__global__ void __launch_bounds__(NW * 32)
-    sweep_kernel3(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, DevState* st) {
-    extern __shared__ __align__(32) unsigned char smem_raw[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    uint64_t* wbest = reinterpret_cast<uint64_t*>(smem_raw + 8);  // NW <= 8
-    OrderedCity* cols = reinterpret_cast<OrderedCity*>(smem_raw + 80);
-
-    if (*(volatile unsigned int*)&st->converged) return;
-    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
-    const uint2 tile = tiles[blockIdx.x];
-    const uint32_t row0 = tile.x, col0 = tile.y;
-    const uint32_t col_end = min(col0 + cb, n);
-    const uint32_t ncols = col_end - col0 + 1;
-
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = ncols * (uint32_t)sizeof(OrderedCity);
-        mbar_arrive_expect_tx(bar, bytes);
-        bulk_g2s(cols, Q + (col0 - 1), bytes, bar);
-    }
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t ib = row0 + (warp * 32 + lane) * R;
-    uint64_t best = kNoMove;
-    int B = -1;
-    {
-        const uint64_t gk = *(volatile unsigned long long*)&st->best_key;
-        if (gk != kNoMove) B = min(B, key_delta(gk));
-    }
-    RowBlock3<R> rb;
-    load_rows3<R>(rb, Q, ib, n);
-    refresh_thresholds3<R>(rb, Q, ib, n, B);
-    if (mbar_wait_bounded(bar, 0, &st->status))
-        walk_columns3<R>(rb, cols, col0 - 1, col0, col_end, ib, n, Q, B, best);
-
-    best = warp_min_u64(best);
-    if (lane == 0) wbest[warp] = best;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t m = wbest[0];
-#pragma unroll
-        for (int w = 1; w < NW; ++w) m = wbest[w] < m ? wbest[w] : m;
-        if (m != kNoMove) atomicMin(&st->best_key, (unsigned long long)m);
-    }
-}
-
-// Packed square-root-free variant (sweep_core4.cuh): the staged tile is
-// re-laid out as broadcast records plus the largest edge of every 32-column
-// window.
-__host__ __device__ constexpr size_t sweep4_cols_offset(uint32_t cb) {
-    return (96 + (size_t)(cb + 1) * sizeof(OrderedCity) + 31) & ~(size_t)31;
-}
-__host__ __device__ constexpr size_t sweep4_wmax_offset(uint32_t cb) {
-    return sweep4_cols_offset(cb) + (size_t)(cb + 1) * sizeof(ColRec);
-}
-
-template <int R, int NW>
-__global__ void __launch_bounds__(NW * 32)
-    sweep_kernel4(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, DevState* st) {
-    extern __shared__ __align__(32) unsigned char smem_raw[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    uint64_t* wbest = reinterpret_cast<uint64_t*>(smem_raw + 8);  // NW <= 8
-    OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
-    ColRec* cols = reinterpret_cast<ColRec*>(smem_raw + sweep4_cols_offset(cb));
-    float* wmax = reinterpret_cast<float*>(smem_raw + sweep4_wmax_offset(cb));
-
-    if (*(volatile unsigned int*)&st->converged) return;
-    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
-    const uint2 tile = tiles[blockIdx.x];
-    const uint32_t row0 = tile.x, col0 = tile.y;
-    const uint32_t col_end = min(col0 + cb, n);
-    const uint32_t ncols = col_end - col0 + 1;
-
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = ncols * (uint32_t)sizeof(OrderedCity);
-        mbar_arrive_expect_tx(bar, bytes);
-        bulk_g2s(stage, Q + (col0 - 1), bytes, bar);
-    }
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t ib = row0 + (warp * 32 + lane) * R;
-    uint64_t best = kNoMove;
-    int B = -1;
-    {
-        const uint64_t gk = *(volatile unsigned long long*)&st->best_key;
-        if (gk != kNoMove) B = min(B, key_delta(gk));
-    }
-    RowBlock4<R> rb;
-    load_rows4<R>(rb, Q, ib, n);
-    refresh4<R>(rb, Q, ib, n, B);
-    const bool staged = mbar_wait_bounded(bar, 0, &st->status);
-    const uint32_t nwin = (col_end - col0 + kWin - 1) / kWin;
-    if (staged) {
-        for (uint32_t k = threadIdx.x; k < ncols; k += NW * 32) cols[k] = make_colrec(stage[k]);
-        for (uint32_t w = threadIdx.x; w < nwin; w += NW * 32) {
-            const uint32_t a = 1 + w * kWin, b = min(a + kWin, ncols);
-            float m = 0.f;
-            for (uint32_t k = a; k < b; ++k) m = fmaxf(m, stage[k].e);
-            wmax[w] = m;
-        }
-    }
-    __syncthreads();
-    if (staged)
-        walk_columns4<R>(rb, cols, col0 - 1, wmax, col0, col0, col_end, ib, n, Q, B, best);
 
     best = warp_min_u64(best);
     if (lane == 0) wbest[warp] = best;
@@ -716,74 +586,7 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
     if (lane == 0 && k != kNoMove) atomicMin(&st->best_key, (unsigned long long)k);
 }
 
-__host__ __device__ constexpr size_t sweep2_cols_offset(uint32_t cb) {
-    return (96 + (size_t)(cb + 1) * sizeof(OrderedCity) + 31) & ~(size_t)31;
-}
-
-// Packed variant: the staged tile is re-laid out in shared memory as 32-byte
-// broadcast records (sweep_core2.cuh) so the fast path issues f32x2 FFMA2 /
-// FMUL2 / FADD2 for two rows at a time.
-template <int R, int NW>
-__global__ void __launch_bounds__(NW * 32)
-    sweep_kernel2(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, float margin,
-                  DevState* st) {
-    extern __shared__ __align__(32) unsigned char smem_raw[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    uint64_t* wbest = reinterpret_cast<uint64_t*>(smem_raw + 8);  // NW <= 8
-    OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
-    ColRec* cols = reinterpret_cast<ColRec*>(smem_raw + sweep2_cols_offset(cb));
-
-    if (*(volatile unsigned int*)&st->converged) return;
-    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
-    const uint2 tile = tiles[blockIdx.x];
-    const uint32_t row0 = tile.x, col0 = tile.y;
-    const uint32_t col_end = min(col0 + cb, n);
-    const uint32_t ncols = col_end - col0 + 1;
-
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = ncols * (uint32_t)sizeof(OrderedCity);
-        mbar_arrive_expect_tx(bar, bytes);
-        bulk_g2s(stage, Q + (col0 - 1), bytes, bar);
-    }
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t ib = row0 + (warp * 32 + lane) * R;
-    uint64_t best = kNoMove;
-    int B = -1;
-    {
-        const uint64_t gk = *(volatile unsigned long long*)&st->best_key;
-        if (gk != kNoMove) B = min(B, key_delta(gk));
-    }
-    RowBlock2<R> rb;
-    load_rows2<R>(rb, Q, ib, n);
-    refresh_thresholds2<R>(rb, Q, ib, n, B, margin);
-    const bool staged = mbar_wait_bounded(bar, 0, &st->status);
-    if (staged)
-        for (uint32_t k = threadIdx.x; k < ncols; k += NW * 32) cols[k] = make_colrec(stage[k]);
-    __syncthreads();
-    if (staged)
-        walk_columns2<R>(rb, cols, col0 - 1, col0, col_end, ib, n, Q, margin, B, best);
-
-    best = warp_min_u64(best);
-    if (lane == 0) wbest[warp] = best;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t m = wbest[0];
-#pragma unroll
-        for (int w = 1; w < NW; ++w) m = wbest[w] < m ? wbest[w] : m;
-        if (m != kNoMove) atomicMin(&st->best_key, (unsigned long long)m);
-    }
-}
-
 size_t sweep_smem_bytes(uint32_t cb) { return 80 + (size_t)(cb + 1) * sizeof(OrderedCity); }
-size_t sweep2_smem_bytes(uint32_t cb) {
-    return sweep2_cols_offset(cb) + (size_t)(cb + 1) * sizeof(ColRec);
-}
 
 // The dynamic shared-memory limit is a property of the kernel, shared by
 // every context in the process: it is always set for the largest tile a
@@ -792,35 +595,6 @@ size_t sweep2_smem_bytes(uint32_t cb) {
 constexpr uint32_t kMaxTileCols = 4096;
 constexpr uint32_t kMaxBoxedCols = 1024;  // one mask bit per 32-column window
 inline int attr_bytes(size_t smem) { return (int)(smem > 48 * 1024 ? smem : 48 * 1024); }
-
-template <int R, int NW>
-static cudaError_t launch_sweep2_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
-    const size_t smem = sweep2_smem_bytes(L.cb);
-    if (prepare) {
-        return cudaFuncSetAttribute(sweep_kernel2<R, NW>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    attr_bytes(sweep2_smem_bytes(kMaxTileCols)));
-    }
-    sweep_kernel2<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
-                                                         L.margin, L.st);
-    return cudaGetLastError();
-}
-
-size_t sweep4_smem_bytes(uint32_t cb) {
-    return sweep4_wmax_offset(cb) + ((size_t)cb / kWin + 2) * sizeof(float);
-}
-
-template <int R, int NW>
-static cudaError_t launch_sweep4_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
-    const size_t smem = sweep4_smem_bytes(L.cb);
-    if (prepare) {
-        return cudaFuncSetAttribute(sweep_kernel4<R, NW>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    attr_bytes(sweep4_smem_bytes(kMaxTileCols)));
-    }
-    sweep_kernel4<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb, L.st);
-    return cudaGetLastError();
-}
 
 size_t sweep5_smem_bytes(uint32_t cb) {
     return sweep5_wmax_offset(cb) + ((size_t)cb / kWin5 + 2) * sizeof(float);
@@ -928,18 +702,6 @@ static cudaError_t launch_sweep6_t(const SweepLaunch& L, cudaStream_t s, bool pr
 }
 
 template <int R, int NW>
-static cudaError_t launch_sweep3_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
-    const size_t smem = sweep_smem_bytes(L.cb);
-    if (prepare) {
-        return cudaFuncSetAttribute(sweep_kernel3<R, NW>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    attr_bytes(sweep_smem_bytes(kMaxTileCols)));
-    }
-    sweep_kernel3<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb, L.st);
-    return cudaGetLastError();
-}
-
-template <int R, int NW>
 static cudaError_t launch_sweep_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     const size_t smem = sweep_smem_bytes(L.cb);
     if (prepare) {
@@ -988,37 +750,6 @@ static cudaError_t dispatch_sweep(const SweepLaunch& L, cudaStream_t s, bool pre
             default: return cudaErrorInvalidValue;
         }
     }
-    if (L.variant == 3) {
-        switch (L.R * 100 + L.NW) {
-            case 404: return launch_sweep4_t<4, 4>(L, s, prepare);
-            case 804: return launch_sweep4_t<8, 4>(L, s, prepare);
-            case 808: return launch_sweep4_t<8, 8>(L, s, prepare);
-            case 1604: return launch_sweep4_t<16, 4>(L, s, prepare);
-            default: return cudaErrorInvalidValue;
-        }
-    }
-    if (L.variant == 2) {
-        switch (L.R * 100 + L.NW) {
-            case 202: return launch_sweep3_t<2, 2>(L, s, prepare);
-            case 402: return launch_sweep3_t<4, 2>(L, s, prepare);
-            case 404: return launch_sweep3_t<4, 4>(L, s, prepare);
-            case 804: return launch_sweep3_t<8, 4>(L, s, prepare);
-            case 808: return launch_sweep3_t<8, 8>(L, s, prepare);
-            case 1604: return launch_sweep3_t<16, 4>(L, s, prepare);
-            default: return cudaErrorInvalidValue;
-        }
-    }
-    if (L.variant == 1) {
-        switch (L.R * 100 + L.NW) {
-            case 402: return launch_sweep2_t<4, 2>(L, s, prepare);
-            case 404: return launch_sweep2_t<4, 4>(L, s, prepare);
-            case 804: return launch_sweep2_t<8, 4>(L, s, prepare);
-            case 808: return launch_sweep2_t<8, 8>(L, s, prepare);
-            case 1602: return launch_sweep2_t<16, 2>(L, s, prepare);
-            case 1604: return launch_sweep2_t<16, 4>(L, s, prepare);
-            default: return cudaErrorInvalidValue;
-        }
-    }
     switch (L.R * 100 + L.NW) {
         case 202: return launch_sweep_t<2, 2>(L, s, prepare);
         case 204: return launch_sweep_t<2, 4>(L, s, prepare);
@@ -1042,6 +773,7 @@ cudaError_t launch_sweep_prepare(const SweepLaunch& L) {
 }
 
 bool sweep_shape_supported(int R, int NW, int variant) {
+    if (variant < 0 || variant > 6 || (variant >= 1 && variant <= 3)) return false;
     if (variant == 5 || variant == 6) {
         switch (R * 100 + NW) {
             case 402: case 404: case 408: case 804: case 808: case 1604:
@@ -1053,30 +785,6 @@ bool sweep_shape_supported(int R, int NW, int variant) {
     if (variant == 4) {
         switch (R * 100 + NW) {
             case 402: case 404: case 408: case 802: case 804: case 808: case 1604:
-                return true;
-            default:
-                return false;
-        }
-    }
-    if (variant == 3) {
-        switch (R * 100 + NW) {
-            case 404: case 804: case 808: case 1604:
-                return true;
-            default:
-                return false;
-        }
-    }
-    if (variant == 2) {
-        switch (R * 100 + NW) {
-            case 202: case 402: case 404: case 804: case 808: case 1604:
-                return true;
-            default:
-                return false;
-        }
-    }
-    if (variant == 1) {
-        switch (R * 100 + NW) {
-            case 402: case 404: case 804: case 808: case 1602: case 1604:
                 return true;
             default:
                 return false;

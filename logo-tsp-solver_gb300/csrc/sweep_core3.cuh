@@ -1,4 +1,5 @@
-// Square-root-free fast path of the sweep (the default single-instance core).
+// Square-root-free bound of the sweep screens (used by the fused, local and
+// boxed screens and the batched CTA sweep).
 //
 // A pair (i, c) can only be chosen if its exact delta is <= B, the best exact
 // delta this thread has seen (B <= -1).  With d1 = nint d(i, c) and
@@ -11,12 +12,12 @@
 //     L = RN(u * |u|),  u = V + 5,
 // for every V <= 1.6e7 (here V <= 4e6: the coordinate box diagonal is below
 // 2e6, so every edge is below 2e6).  A negative u makes L negative, so such
-// pairs never pass.  The fast path therefore computes one sum of squares per
+// pairs never pass.  A screen therefore needs one sum of squares per
 // distance-matrix entry (each entry serves two pairs) and, per pair,
-//     u = T2[r] + e_c,  L = u * |u|,  max(s(i,c), s(i-1,c-1)) < L
-// with T2[r] = B + e[i] + 5 -- no square root and no MUFU work.  Columns with
-// a passing pair are re-evaluated exactly (exact_dist), exactly as the other
-// cores do, so the chosen move is still the exact lowest (delta, i, c).
+//     u = B + e[i] + 5 + e_c,  L = u * |u|,  max(s(i,c), s(i-1,c-1)) < L
+// -- no square root and no MUFU work.  Pairs that pass are re-evaluated
+// exactly (exact_dist), so the chosen move is still the exact lowest
+// (delta, i, c).
 #pragma once
 #include "logo_device.cuh"
 
@@ -26,108 +27,6 @@ __device__ __forceinline__ float sq_dist(float ax, float ay, float bx, float by)
     const float dx = ax - bx;
     const float dy = ay - by;
     return __fmaf_rn(dy, dy, dx * dx);
-}
-
-template <int R>
-struct RowBlock3 {
-    float x[R + 1], y[R + 1];  // rows ib-1 .. ib+R-1
-    float T2[R];               // B + e[ib+r] + 5 (exact integers)
-    float Sp[R];               // s(ib-1+r, c-1)
-};
-
-template <int R>
-__device__ __forceinline__ void load_rows3(RowBlock3<R>& rb, const OrderedCity* Q, uint32_t ib,
-                                           uint32_t n) {
-#pragma unroll
-    for (int k = 0; k <= R; ++k) {
-        const uint32_t idx = min(ib - 1 + k, n - 1);
-        const float4 p = *reinterpret_cast<const float4*>(Q + idx);
-        rb.x[k] = p.x;
-        rb.y[k] = p.y;
-    }
-}
-
-template <int R>
-__device__ __forceinline__ void refresh_thresholds3(RowBlock3<R>& rb, const OrderedCity* Q,
-                                                    uint32_t ib, uint32_t n, int B) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const uint32_t i = ib + r;
-        // rows past n-3 hold no pair: a very negative T2 makes u < 0
-        rb.T2[r] = (i + 3 <= n) ? (float)(B + (int)Q[i].e + 5) : -3.0e7f;
-    }
-}
-
-template <int R>
-__device__ __forceinline__ void column_exact3(RowBlock3<R>& rb, const float* S,
-                                              const OrderedCity& q, const OrderedCity& qp,
-                                              uint32_t c, uint32_t ib, uint32_t n,
-                                              const OrderedCity* Q, int& B, uint64_t& best) {
-    const int ec = (int)q.e;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const uint32_t i = ib + r;
-        const float u = rb.T2[r] + q.e;
-        const float L = u * fabsf(u);
-        if (c >= i + 2 && fmaxf(S[r + 1], rb.Sp[r]) < L) {
-            const int d1 = exact_dist(rb.x[r + 1], rb.y[r + 1], q.x, q.y);
-            const int d2 = exact_dist(rb.x[r], rb.y[r], qp.x, qp.y);
-            const int ei = (int)Q[i].e;
-            const int delta = d1 + d2 - ei - ec;
-            if (delta <= B) {
-                const uint64_t key = pack_key(delta, i, c);
-                best = key < best ? key : best;
-                if (delta < B) {
-                    B = delta;
-                    refresh_thresholds3<R>(rb, Q, ib, n, B);
-                }
-            }
-        }
-    }
-}
-
-template <int R, bool MASK>
-__device__ __forceinline__ void column_step3(RowBlock3<R>& rb, const OrderedCity* cols,
-                                             uint32_t base, uint32_t c, uint32_t ib, uint32_t n,
-                                             const OrderedCity* Q, int& B, uint64_t& best) {
-    const OrderedCity q = cols[c - base];
-    float S[R + 1];
-#pragma unroll
-    for (int k = 0; k <= R; ++k) S[k] = sq_dist(rb.x[k], rb.y[k], q.x, q.y);
-    bool hit = false;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const float u = rb.T2[r] + q.e;
-        const float L = u * fabsf(u);
-        const bool cand = fmaxf(S[r + 1], rb.Sp[r]) < L;
-        if (MASK)
-            hit |= cand && (c >= ib + r + 2);
-        else
-            hit |= cand;
-    }
-    if (hit) {
-        const OrderedCity qp = cols[c - base - 1];
-        column_exact3<R>(rb, S, q, qp, c, ib, n, Q, B, best);
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r) rb.Sp[r] = S[r];
-}
-
-template <int R>
-__device__ __forceinline__ void walk_columns3(RowBlock3<R>& rb, const OrderedCity* cols,
-                                              uint32_t base, uint32_t c_lo, uint32_t c_hi,
-                                              uint32_t ib, uint32_t n, const OrderedCity* Q,
-                                              int& B, uint64_t& best) {
-    const uint32_t c_first = max(c_lo, ib + 2);
-    if (ib + 3 > n || c_first >= c_hi) return;
-    const OrderedCity pc = cols[c_first - base - 1];
-#pragma unroll
-    for (int r = 0; r < R; ++r) rb.Sp[r] = sq_dist(rb.x[r], rb.y[r], pc.x, pc.y);
-    uint32_t c = c_first;
-    const uint32_t peel_end = min(c_hi, ib + R + 1);
-    for (; c < peel_end; ++c) column_step3<R, true>(rb, cols, base, c, ib, n, Q, B, best);
-#pragma unroll 2
-    for (; c < c_hi; ++c) column_step3<R, false>(rb, cols, base, c, ib, n, Q, B, best);
 }
 
 }  // namespace logo

@@ -22,9 +22,6 @@ LIB_PATH = os.path.join(HERE, "liblogo_gpu.so")
 KICK_SEGMENT = 0
 KICK_DOUBLE_BRIDGE = 1
 SWEEP_MUFU = 0
-SWEEP_MUFU_PACKED = 1
-SWEEP_SQUARED = 2
-SWEEP_SQUARED_PACKED = 3
 SWEEP_FUSED = 4
 SWEEP_LOCAL = 5
 SWEEP_BOXED = 6

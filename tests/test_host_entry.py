@@ -7,7 +7,8 @@ import numpy as np
 import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_TSPLIB = "/root/reference/TSPLIB"
+# the reference checkout (the same REF variable oracle/build_ref.sh reads)
+REF_TSPLIB = os.path.join(os.environ.get("REF", "/root/reference"), "TSPLIB")
 GENS = ["uniform_int", "uniform_f32", "clustered"]
 
 

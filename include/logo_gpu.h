@@ -129,11 +129,11 @@ logo_status logo_ils(logo_ctx *ctx, uint32_t *route_inout, uint32_t kicks,
 logo_status logo_tour_length(logo_ctx *ctx, const uint32_t *route, uint64_t *length);
 
 /* logo_descend that also records every applied move as (minchange, i, j)
- * int32 triples into trace[0 .. 3*trace_cap) -- the per-move report that
+ * int32 triples into move_log[0 .. 3*log_cap) -- the per-move report that
  * TwoOptLocalSolver::optimize prints when showLocalOptimizationInfo is set
  * (src/solvers/twoOptLocalSolver.cpp:56-65). */
 logo_status logo_descend_trace(logo_ctx *ctx, uint32_t *route_inout, uint64_t max_moves,
-                               int32_t *trace, uint64_t trace_cap, logo_stats *stats);
+                               int32_t *move_log, uint64_t log_cap, logo_stats *stats);
 
 /* ---- allocation-free sweep ----------------------------------------------------- */
 
@@ -436,6 +436,8 @@ typedef struct logo_ctx_info {
     int variant;          /* LOGO_SWEEP_* */
     int descent_mode;     /* LOGO_DESCENT_* in use */
     int cooperative_ctas; /* CTAs of the cooperative descent; 0 if unavailable */
+    uint64_t host_waits;  /* times this context's calls have waited on the device so far
+                             (one logo_ils call: a fixed handful, whatever the kick count) */
 } logo_ctx_info;
 
 logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
@@ -508,6 +510,14 @@ const char *logo_version(void);
  * pair took.  Nothing faults or hangs; the device stays usable. */
 logo_status logo_diag_wait_limits(int device, uint32_t *mbarrier_status,
                                   uint32_t *barrier_status, double *waited_ms);
+
+/* Test hook for the host side of a device timeout (no counterpart in the
+ * reference): sets the timeout bit in the context's device status word, as a
+ * sweep wait or the cooperative grid barrier does when it gives up, without
+ * any wait running out.  The next call that reads the status returns
+ * LOGO_ERR_TIMEOUT and every later call on the context LOGO_ERR_DEVICE_FAULT
+ * (a context whose device wait timed out is never used again; destroy it). */
+logo_status logo_diag_flag_timeout(logo_ctx *ctx);
 
 /* Self-check of the sweep's exactness argument: the largest relative error of
  * the device's approximate square root over every positive normal binary32

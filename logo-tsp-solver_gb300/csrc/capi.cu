@@ -40,8 +40,11 @@ struct logo_ctx {
     float* d_rmax = nullptr;
     uint4* d_work = nullptr;      // boxed sweep: tiles that pass the window test
     uint32_t* d_workctl = nullptr;
+    uint32_t* d_pos = nullptr;    // boxed sweep: tour position of every city
+    uint32_t* d_nbr = nullptr;    // boxed sweep: kSeedNeighbours nearest cities per city
     CoopSync* d_coop = nullptr;   // barrier and best-key slots of the cooperative descent
     int coop_grid = 0;            // CTAs of the cooperative descent (0: unavailable)
+    int coop_ils_grid = 0;        // CTAs of the cooperative ILS launch (0: unavailable)
     int descent_mode = LOGO_DESCENT_AUTO;
     uint2* d_tiles = nullptr;
     uint32_t ntiles = 0;
@@ -51,9 +54,12 @@ struct logo_ctx {
     float margin = 0.f;
     double diag = 0.0;
     cudaGraphExec_t chunk_exec = nullptr;
+    cudaGraphExec_t ils_exec = nullptr;  // device-run ILS (graph descent path), built on first use
     uint32_t chunk_steps = 8;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool have_route = false;
+    uint64_t host_waits = 0;      // stream/event synchronisations made for this context
+    bool poisoned = false;        // a device-side wait timed out: the context is not used again
     std::string err;
 };
 
@@ -114,6 +120,10 @@ SweepLaunch sweep_args(const logo_ctx* c) {
     L.rmax = c->d_rmax;
     L.work = c->d_work;
     L.workctl = c->d_workctl;
+    L.R0 = c->d_route[0];
+    L.R1 = c->d_route[1];
+    L.pos = c->d_pos;
+    L.nbr = c->d_nbr;
     return L;
 }
 
@@ -186,6 +196,10 @@ logo_status rebuild(logo_ctx* c) {
         cudaGraphExecDestroy(c->chunk_exec);
         c->chunk_exec = nullptr;
     }
+    if (c->ils_exec) {
+        cudaGraphExecDestroy(c->ils_exec);
+        c->ils_exec = nullptr;
+    }
     if (c->d_tiles) {
         cudaFree(c->d_tiles);
         c->d_tiles = nullptr;
@@ -193,6 +207,18 @@ logo_status rebuild(logo_ctx* c) {
     if (c->d_work) {
         cudaFree(c->d_work);
         c->d_work = nullptr;
+    }
+    if (c->variant == LOGO_SWEEP_BOXED && !c->d_nbr) {
+        // near neighbours of every city, once per context: the boxed sweep's
+        // seed pass evaluates their pairs first (host grid search)
+        std::vector<logo_xy> h(c->n);
+        CK(c, cudaMemcpy(h.data(), c->d_xy, sizeof(logo_xy) * c->n, cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> nb((size_t)c->n * kSeedNeighbours);
+        knn_grid(h.data(), c->n, kSeedNeighbours, nb.data());
+        CK(c, cudaMalloc(&c->d_pos, sizeof(uint32_t) * c->n));
+        CK(c, cudaMalloc(&c->d_nbr, sizeof(uint32_t) * nb.size()));
+        CK(c, cudaMemcpy(c->d_nbr, nb.data(), sizeof(uint32_t) * nb.size(),
+                         cudaMemcpyHostToDevice));
     }
     std::vector<uint2> tiles = make_tiles(c->n, c->R, c->NW, c->cb);
     c->ntiles = (uint32_t)tiles.size();
@@ -227,6 +253,129 @@ logo_status rebuild(logo_ctx* c) {
     return LOGO_OK;
 }
 
+// ---- device-run ILS graph ---------------------------------------------------
+// One graph runs a whole ILS call (ILSGlobalSolverSequential::optimize,
+// src/solvers/ILSGlobalSolverSequential.cpp:60-100, with a kick count):
+//
+//   descent_cond(first) ; WHILE(d) { chunk_steps x (sweep, apply) ; descent_cond }
+//   length ; accept ; kick_cond(first)
+//   WHILE(k) { kick ; descent_cond(first) ; WHILE(d2) { ... } ; length ; accept ; kick_cond }
+//
+// so the host launches it once and synchronises once per call.  Every loop
+// is bounded on the device (descent_cond_kernel / kick_cond_kernel).
+
+// Adds a WHILE node on handle h at the capture position of stream s and
+// captures its body, built by body(bs), on stream bs.
+template <typename F>
+cudaError_t capture_while(cudaStream_t s, cudaGraphConditionalHandle h, cudaStream_t bs,
+                          F body) {
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    if (cst != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureInvalidated;
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(bs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t eb = body(bs);
+    cudaGraph_t out = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(bs, &out);
+    return eb != cudaSuccess ? eb : ee;
+}
+
+// The graph currently captured on stream s (for handle creation).
+cudaError_t capturing_graph(cudaStream_t s, cudaGraph_t* g) {
+    cudaStreamCaptureStatus cst;
+    return cudaStreamGetCaptureInfo(s, &cst, nullptr, g, nullptr, nullptr, nullptr);
+}
+
+// descent_cond(first) + WHILE(h) { chunk_steps x (sweep, apply) + descent_cond }
+// at the capture position of s (graph g holds the WHILE node); bs captures the body.
+cudaError_t capture_descent_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
+                                 cudaStream_t bs) {
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+    if (e != cudaSuccess) return e;
+    e = launch_descent_cond(c->d_st, h, true, s);
+    if (e != cudaSuccess) return e;
+    const SweepLaunch L = sweep_args(c);
+    const TourBufs T = bufs(c);
+    const uint32_t steps = c->chunk_steps;
+    DevState* st = c->d_st;
+    return capture_while(s, h, bs, [&](cudaStream_t b) {
+        cudaError_t eb = cudaSuccess;
+        for (uint32_t k = 0; k < steps && eb == cudaSuccess; ++k) {
+            eb = launch_sweep(L, b);
+            if (eb == cudaSuccess) eb = launch_apply_move(T, b);
+        }
+        if (eb == cudaSuccess) eb = launch_descent_cond(st, h, false, b);
+        return eb;
+    });
+}
+
+logo_status build_ils_graph(logo_ctx* c) {
+    if (c->ils_exec) return LOGO_OK;
+    cudaStream_t s2 = nullptr, s3 = nullptr;
+    CK(c, cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    if (cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(s2);
+        return fail(c, LOGO_ERR_CUDA, "stream creation failed");
+    }
+    const TourBufs T = bufs(c);
+    DevState* st = c->d_st;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    cudaGraph_t top = nullptr;
+    if (e == cudaSuccess) e = capturing_graph(c->stream, &top);
+    if (e == cudaSuccess) e = capture_descent_loop(c, c->stream, top, s2);
+    if (e == cudaSuccess) e = launch_tour_length(T, c->stream);
+    if (e == cudaSuccess) e = launch_accept(T, c->stream);
+    cudaGraphConditionalHandle hk;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hk, top, 0, 0);
+    if (e == cudaSuccess) e = launch_kick_cond(st, hk, true, c->stream);
+    if (e == cudaSuccess)
+        e = capture_while(c->stream, hk, s2, [&](cudaStream_t b) {
+            cudaError_t eb = launch_kick_dev(T, b);
+            cudaGraph_t body = nullptr;
+            if (eb == cudaSuccess) eb = capturing_graph(b, &body);
+            if (eb == cudaSuccess) eb = capture_descent_loop(c, b, body, s3);
+            if (eb == cudaSuccess) eb = launch_tour_length(T, b);
+            if (eb == cudaSuccess) eb = launch_accept(T, b);
+            if (eb == cudaSuccess) eb = launch_kick_cond(st, hk, false, b);
+            return eb;
+        });
+    const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    cudaStreamDestroy(s2);
+    cudaStreamDestroy(s3);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return fail(c, LOGO_ERR_CUDA,
+                    std::string("ILS graph capture: ") +
+                        cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&c->ils_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->ils_exec = nullptr;
+        return fail(c, LOGO_ERR_CUDA, std::string("ILS graph instantiation: ") +
+                                          cudaGetErrorString(e));
+    }
+    return LOGO_OK;
+}
+
 // Uploads a route and builds the ordered tour.  Whether the route is a
 // permutation of 0..n-1 is checked on the device by the gather (a host
 // check cost about 80 us per call at n = 100k, a tenth of a sweep);
@@ -248,6 +397,7 @@ logo_status upload_route(logo_ctx* c, const uint32_t* route) {
 logo_status read_state(logo_ctx* c) {
     CK(c, cudaMemcpyAsync(c->h_st, c->d_st, sizeof(DevState), cudaMemcpyDeviceToHost,
                           c->stream));
+    ++c->host_waits;
     CK(c, cudaStreamSynchronize(c->stream));
     if (c->h_st->bad_route) {
         c->have_route = false;
@@ -256,9 +406,23 @@ logo_status read_state(logo_ctx* c) {
     return LOGO_OK;
 }
 
+// A device-side wait that gave up (kErrTimeout) may have left a bulk copy
+// in flight into shared memory of a CTA that has already exited, or CTAs of
+// a cooperative grid still running; nothing later on this context can rely
+// on its buffers, so the context refuses every further call except destroy.
+logo_status poisoned_error(logo_ctx* c) {
+    return fail(c, LOGO_ERR_DEVICE_FAULT,
+                "context unusable: a device-side wait timed out earlier; destroy it and "
+                "create a new one");
+}
+
 logo_status status_to_error(logo_ctx* c, unsigned int st) {
-    if (st & kErrTimeout)
-        return fail(c, LOGO_ERR_TIMEOUT, "a device-side wait exceeded its time budget");
+    if (st & kErrTimeout) {
+        c->poisoned = true;
+        return fail(c, LOGO_ERR_TIMEOUT,
+                    "a device-side wait exceeded its time budget; the context is unusable "
+                    "from now on (destroy it)");
+    }
     if (st & kErrBadKey)
         return fail(c, LOGO_ERR_DEVICE_FAULT, "sweep produced an out-of-range move");
     if (st & kErrMoveLimit)
@@ -366,6 +530,7 @@ logo_status download_route(logo_ctx* c, uint32_t* route, bool best) {
     const uint32_t* src = best ? c->d_route_best : c->d_route[c->h_st->cur & 1];
     CK(c, cudaMemcpyAsync(route, src, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToHost,
                           c->stream));
+    ++c->host_waits;
     CK(c, cudaStreamSynchronize(c->stream));
     return LOGO_OK;
 }
@@ -383,6 +548,7 @@ void destroy(logo_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->chunk_exec) cudaGraphExecDestroy(c->chunk_exec);
+    if (c->ils_exec) cudaGraphExecDestroy(c->ils_exec);
     cudaFree(c->d_xy);
     cudaFree(c->d_Q[0]);
     cudaFree(c->d_Q[1]);
@@ -399,6 +565,8 @@ void destroy(logo_ctx* c) {
     cudaFree(c->d_rmax);
     cudaFree(c->d_work);
     cudaFree(c->d_workctl);
+    cudaFree(c->d_pos);
+    cudaFree(c->d_nbr);
     cudaFree(c->d_coop);
     if (c->h_st) cudaFreeHost(c->h_st);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -412,6 +580,7 @@ struct Timer {
     explicit Timer(logo_ctx* cc) : c(cc) { cudaEventRecord(c->ev0, c->stream); }
     double stop() {
         cudaEventRecord(c->ev1, c->stream);
+        ++c->host_waits;
         cudaEventSynchronize(c->ev1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -519,6 +688,7 @@ logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_
     CKC(cudaMalloc(&c->d_rmax, sizeof(float) * sweep_row_windows(n)));
     CKC(cudaMalloc(&c->d_workctl, 2 * sizeof(uint32_t)));
     c->coop_grid = coop_grid(n, device);
+    c->coop_ils_grid = c->coop_grid > 0 ? coop_ils_grid(n, device) : 0;
     if (c->coop_grid > 0) CKC(cudaMalloc(&c->d_coop, sizeof(CoopSync)));
     std::memset(c->h_st, 0, sizeof(DevState));
     c->h_st->best_key = kNoMove;
@@ -550,11 +720,13 @@ logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
     info->variant = c->variant;
     info->descent_mode = use_coop(c) ? LOGO_DESCENT_COOPERATIVE : LOGO_DESCENT_GRAPH;
     info->cooperative_ctas = c->coop_grid;
+    info->host_waits = c->host_waits;
     return LOGO_OK;
 }
 
 logo_status logo_ctx_set_descent_mode(logo_ctx* c, int mode) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (mode != LOGO_DESCENT_AUTO && mode != LOGO_DESCENT_GRAPH &&
         mode != LOGO_DESCENT_COOPERATIVE)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown descent mode");
@@ -567,6 +739,7 @@ logo_status logo_ctx_set_descent_mode(logo_ctx* c, int mode) {
 
 logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!sweep_shape_supported(R, NW, c->variant) || cb < 16 || cb > 4096 ||
         !sweep_cols_supported(c->variant, cb))
         return fail(c, LOGO_ERR_INVALID_ARG, "unsupported sweep shape");
@@ -580,6 +753,7 @@ logo_status logo_ctx_set_shape(logo_ctx* c, int R, int NW, uint32_t cb) {
 
 logo_status logo_ctx_set_kernel(logo_ctx* c, int variant, int R, int NW, uint32_t cb) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (variant < LOGO_SWEEP_MUFU || variant > LOGO_SWEEP_BOXED ||
         (variant > LOGO_SWEEP_MUFU && variant < LOGO_SWEEP_FUSED))
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown or retired sweep variant");
@@ -599,12 +773,14 @@ void* logo_ctx_stream(logo_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 logo_status logo_sync(logo_ctx* c) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     CK(c, cudaStreamSynchronize(c->stream));
     return LOGO_OK;
 }
 
 logo_status logo_begin_descent(logo_ctx* c, uint64_t max_moves) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     if (max_moves == 0) max_moves = ~0ull >> 1;
@@ -614,6 +790,7 @@ logo_status logo_begin_descent(logo_ctx* c, uint64_t max_moves) {
 
 logo_status logo_enqueue_sweep(logo_ctx* c) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     CK(c, launch_sweep(sweep_args(c), c->stream));
@@ -622,6 +799,7 @@ logo_status logo_enqueue_sweep(logo_ctx* c) {
 
 logo_status logo_enqueue_apply(logo_ctx* c) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     CK(c, launch_apply_move(bufs(c), c->stream));
@@ -630,6 +808,7 @@ logo_status logo_enqueue_apply(logo_ctx* c) {
 
 logo_status logo_get_progress(logo_ctx* c, uint64_t* moves, int* converged) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
     logo_status s = read_state(c);
     if (s != LOGO_OK) return s;
@@ -640,8 +819,19 @@ logo_status logo_get_progress(logo_ctx* c, uint64_t* moves, int* converged) {
     return LOGO_OK;
 }
 
+logo_status logo_diag_flag_timeout(logo_ctx* c) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    CK(c, cudaSetDevice(c->device));
+    const unsigned int bit = kErrTimeout;
+    CK(c, cudaMemcpyAsync(&c->d_st->status, &bit, sizeof(bit), cudaMemcpyHostToDevice,
+                          c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return LOGO_OK;
+}
+
 logo_status logo_set_route(logo_ctx* c, const uint32_t* route) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
     logo_status s = upload_route(c, route);
     if (s != LOGO_OK) return s;
@@ -650,6 +840,7 @@ logo_status logo_set_route(logo_ctx* c, const uint32_t* route) {
 
 logo_status logo_get_route(logo_ctx* c, uint32_t* route) {
     if (!c || !route) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     logo_status s = read_state(c);
@@ -659,6 +850,7 @@ logo_status logo_get_route(logo_ctx* c, uint32_t* route) {
 
 logo_status logo_best_move(logo_ctx* c, const uint32_t* route, logo_move* out) {
     if (!c || !out) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
     logo_status s = upload_route(c, route);
     if (s != LOGO_OK) return s;
@@ -667,6 +859,7 @@ logo_status logo_best_move(logo_ctx* c, const uint32_t* route, logo_move* out) {
 
 logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
     if (!c || !out) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));  // clears status too
@@ -689,6 +882,7 @@ logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
 
 logo_status logo_descend_resident(logo_ctx* c, uint64_t max_moves, logo_stats* stats) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     Timer t(c);
@@ -709,6 +903,7 @@ logo_status logo_descend_resident(logo_ctx* c, uint64_t max_moves, logo_stats* s
 
 logo_status logo_length_resident(logo_ctx* c, uint64_t* len) {
     if (!c || !len) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
     return length_now(c, len);
@@ -716,6 +911,7 @@ logo_status logo_length_resident(logo_ctx* c, uint64_t* len) {
 
 logo_status logo_tour_length(logo_ctx* c, const uint32_t* route, uint64_t* len) {
     if (!c || !len) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
     logo_status s = upload_route(c, route);
     if (s != LOGO_OK) return s;
@@ -725,6 +921,7 @@ logo_status logo_tour_length(logo_ctx* c, const uint32_t* route, uint64_t* len) 
 static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves,
                                 int32_t* trace, uint64_t trace_cap, logo_stats* stats) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
     Timer t(c);
     logo_status s = upload_route(c, route);
@@ -795,36 +992,67 @@ logo_status logo_descend_trace(logo_ctx* c, uint32_t* route, uint64_t max_moves,
 logo_status logo_ils(logo_ctx* c, uint32_t* route, uint32_t kicks, uint64_t seed,
                      int kick_kind, logo_stats* stats) {
     if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
     if (kick_kind != LOGO_KICK_SEGMENT && kick_kind != LOGO_KICK_DOUBLE_BRIDGE)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown kick kind");
     CK(c, cudaSetDevice(c->device));
+    const bool coop = use_coop(c) && c->coop_ils_grid > 0;
+    if (!coop) {
+        logo_status sb = build_ils_graph(c);  // once per context and tile shape
+        if (sb != LOGO_OK) return sb;
+    }
     Timer t(c);
     logo_status s = upload_route(c, route);
     if (s != LOGO_OK) return s;
-    // seed the device PRNG and clear the ILS counters
+    // seed the device PRNG, clear the ILS counters, set the kick count and kind
+    const unsigned long long target = kicks;
+    const unsigned int kind = (unsigned int)kick_kind;
     CK(c, cudaMemcpyAsync(&c->d_st->rng, &seed, sizeof(seed), cudaMemcpyHostToDevice,
+                          c->stream));
+    CK(c, cudaMemcpyAsync(&c->d_st->kick_target, &target, sizeof(target),
+                          cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(&c->d_st->kick_kind, &kind, sizeof(kind), cudaMemcpyHostToDevice,
                           c->stream));
     CK(c, cudaMemsetAsync(&c->d_st->total_moves, 0, sizeof(unsigned long long), c->stream));
     CK(c, cudaMemsetAsync(&c->d_st->accepted, 0, sizeof(unsigned long long), c->stream));
     CK(c, cudaMemsetAsync(&c->d_st->kicks, 0, sizeof(unsigned long long), c->stream));
     CK(c, cudaMemsetAsync(&c->d_st->sweeps, 0, sizeof(unsigned long long), c->stream));
     CK(c, launch_tour_length(bufs(c), c->stream));
-    CK(c, launch_save_best(bufs(c), c->stream));
-    s = read_state(c);
-    if (s != LOGO_OK) return s;
-    const uint64_t start_len = c->h_st->best_length;
+    CK(c, launch_save_best(bufs(c), c->stream));  // best = start, start_length recorded
     const uint64_t kmax = 64ull * c->n * c->n + 1024;
-    for (uint32_t it = 0;; ++it) {
-        s = run_descent(c, kmax, nullptr, nullptr, it == 0);
-        if (s != LOGO_OK) return s;
-        CK(c, launch_tour_length(bufs(c), c->stream));
-        CK(c, launch_accept(bufs(c), c->stream));
-        if (it == kicks) break;
-        CK(c, launch_kick(bufs(c), kick_kind, c->stream));
+    CK(c, launch_reset_descent(bufs(c), kmax, c->stream));
+    if (coop) {
+        // one cooperative launch runs every descent, length, accept and kick
+        CK(c, cudaMemsetAsync(c->d_coop, 0xFF, sizeof(CoopSync), c->stream));
+        CK(c, cudaMemsetAsync(c->d_coop, 0, 2 * sizeof(unsigned int), c->stream));
+        CoopArgs A;
+        A.Q0 = c->d_Q[0];
+        A.Q1 = c->d_Q[1];
+        A.R0 = c->d_route[0];
+        A.R1 = c->d_route[1];
+        A.n = c->n;
+        A.margin = c->margin;
+        A.st = c->d_st;
+        A.cs = c->d_coop;
+        A.xy = c->d_xy;
+        A.Qbest = c->d_Qbest;
+        A.route_best = c->d_route_best;
+        A.kicks = kicks;
+        A.kick_kind = kick_kind;
+        std::lock_guard<std::mutex> lk(coop_lock(c->device));
+        CK(c, launch_coop_ils(A, c->coop_ils_grid, c->stream));
+        s = read_state(c);
+    } else {
+        // one graph: descent and kick loops are WHILE nodes on device conditions
+        CK(c, cudaGraphLaunch(c->ils_exec, c->stream));
+        s = read_state(c);
     }
-    s = read_state(c);
     if (s != LOGO_OK) return s;
     const DevState fin = *c->h_st;
+    const unsigned int st = fin.status & ~kErrMoveLimit;
+    if (st) return status_to_error(c, st);
+    if (!fin.converged || fin.kicks != kicks)
+        return fail(c, LOGO_ERR_DEVICE_FAULT, "device ILS did not finish");
     s = download_route(c, route, true);
     const double ms = t.stop();
     if (s != LOGO_OK) return s;
@@ -836,7 +1064,7 @@ logo_status logo_ils(logo_ctx* c, uint32_t* route, uint32_t kicks, uint64_t seed
         stats->descents = (uint64_t)kicks + 1;
         stats->kicks = fin.kicks;
         stats->accepted = fin.accepted;
-        stats->start_length = start_len;
+        stats->start_length = fin.start_length;
         stats->final_length = fin.best_length;
         stats->device_ms = ms;
     }

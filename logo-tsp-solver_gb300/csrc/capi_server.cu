@@ -103,8 +103,9 @@ private:
 
 constexpr uint64_t kSmallBytesPerCity = sizeof(float2) + 2 * sizeof(uint32_t);
 // device bytes per city of the single-instance path (coordinates, two tour
-// buffers of ordered cities and routes, best tour)
-constexpr uint64_t kLargeBytesPerCity = 8 + 2 * 16 + 2 * 4 + 16 + 4;
+// buffers of ordered cities and routes, best tour, and the boxed sweep's city
+// positions and near-neighbour lists)
+constexpr uint64_t kLargeBytesPerCity = 8 + 2 * 16 + 2 * 4 + 16 + 4 + 4 * (1 + kSeedNeighbours);
 
 thread_local std::string g_server_err;
 

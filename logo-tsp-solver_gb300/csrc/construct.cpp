@@ -265,6 +265,86 @@ std::string header_value(const std::string& s, size_t colon) {
 
 }  // namespace
 
+namespace logo {
+
+// k nearest other cities of every city (by squared double distance, ties to
+// the lower id), written as out[v * k + j], nearest first; fewer than k
+// other cities leave the remaining slots at the nearest one found (or v
+// itself when n == 1).  A uniform grid of about two cities per cell; each
+// query scans square rings of cells until k candidates are held and the
+// next ring is farther than the k-th.  Used only to seed the sweep's bound
+// with near-neighbour pairs, so any valid neighbour set keeps results exact.
+void knn_grid(const logo_xy* p, uint32_t n, uint32_t k, uint32_t* out) {
+    if (n == 0 || k == 0) return;
+    double x0 = p[0].x, x1 = p[0].x, y0 = p[0].y, y1 = p[0].y;
+    for (uint32_t v = 1; v < n; ++v) {
+        x0 = std::min<double>(x0, p[v].x); x1 = std::max<double>(x1, p[v].x);
+        y0 = std::min<double>(y0, p[v].y); y1 = std::max<double>(y1, p[v].y);
+    }
+    const double w = std::max(x1 - x0, 1e-9), h = std::max(y1 - y0, 1e-9);
+    double cell = std::sqrt(w * h * 2.0 / (double)n);
+    if (!(cell > 0)) cell = std::max(w, h);
+    const uint32_t gw = (uint32_t)std::min<double>(4096.0, std::floor(w / cell) + 1);
+    const uint32_t gh = (uint32_t)std::min<double>(4096.0, std::floor(h / cell) + 1);
+    const double cw = w / gw, ch = h / gh;
+    auto cx_of = [&](double x) {
+        const double t = std::floor((x - x0) / cw);
+        return (uint32_t)std::min<double>(gw - 1, std::max(0.0, t));
+    };
+    auto cy_of = [&](double y) {
+        const double t = std::floor((y - y0) / ch);
+        return (uint32_t)std::min<double>(gh - 1, std::max(0.0, t));
+    };
+    std::vector<uint32_t> start((size_t)gw * gh + 1, 0), items(n);
+    std::vector<uint32_t> cellof(n);
+    for (uint32_t v = 0; v < n; ++v) {
+        cellof[v] = cy_of(p[v].y) * gw + cx_of(p[v].x);
+        start[cellof[v] + 1]++;
+    }
+    for (size_t c = 0; c < (size_t)gw * gh; ++c) start[c + 1] += start[c];
+    {
+        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+        for (uint32_t v = 0; v < n; ++v) items[fill[cellof[v]]++] = v;
+    }
+    std::vector<std::pair<double, uint32_t>> best;
+    best.reserve(k + 1);
+    for (uint32_t v = 0; v < n; ++v) {
+        const double px = p[v].x, py = p[v].y;
+        const int cx = (int)cx_of(px), cy = (int)cy_of(py);
+        best.clear();
+        auto offer = [&](uint32_t u) {
+            if (u == v) return;
+            const double dx = px - (double)p[u].x, dy = py - (double)p[u].y;
+            const std::pair<double, uint32_t> e(dx * dx + dy * dy, u);
+            if (best.size() == k && !(e < best.back())) return;
+            best.insert(std::upper_bound(best.begin(), best.end(), e), e);
+            if (best.size() > k) best.pop_back();
+        };
+        for (int r = 0;; ++r) {
+            // cells of ring r: Chebyshev distance r from (cx, cy)
+            for (int yy = cy - r; yy <= cy + r; ++yy) {
+                if (yy < 0 || yy >= (int)gh) continue;
+                const bool edge_row = (yy == cy - r || yy == cy + r);
+                for (int xx = cx - r; xx <= cx + r; xx += (edge_row ? 1 : 2 * r)) {
+                    if (xx >= 0 && xx < (int)gw) {
+                        const size_t c = (size_t)yy * gw + xx;
+                        for (uint32_t t = start[c]; t < start[c + 1]; ++t) offer(items[t]);
+                    }
+                    if (r == 0) break;
+                }
+            }
+            // every unscanned city is at least r cells away on one axis
+            const double reach = r * std::min(cw, ch);
+            if (best.size() == k && reach * reach > best.back().first) break;
+            if (r > (int)(gw + gh)) break;
+        }
+        for (uint32_t j = 0; j < k; ++j)
+            out[(size_t)v * k + j] = best.empty() ? v : best[std::min<size_t>(j, best.size() - 1)].second;
+    }
+}
+
+}  // namespace logo
+
 extern "C" {
 
 logo_status logo_nn_tour(const logo_xy* coords, uint32_t n, uint32_t start, uint32_t* route) {

@@ -18,9 +18,11 @@
 // log, kErrMoveLimit at max_moves, kErrBadKey on an out-of-range key.  The
 // final tour is written back to buffer `cur` by CTA 0.
 //
-// Best-key slots rotate over three entries: move m uses slot m % 3, and
-// before arriving at barrier m CTA 0 clears slot (m + 1) % 3, which every CTA
-// finished reading before it arrived at barrier m - 1.  Barrier waits are
+// Best-key slots rotate over three entries: sweep s of the launch uses slot
+// s % 3, and before arriving at barrier s CTA 0 clears slot (s + 1) % 3,
+// which every CTA finished reading before it arrived at barrier s - 1.
+// Counting sweeps rather than moves lets one launch run several descents
+// back to back (the ILS launch: descent, length, accept/revert, kick, ...).  Barrier waits are
 // bounded (2 s of %globaltimer); a CTA that gives up sets kErrTimeout and
 // leaves the loop, so the others give up too and the launch ends.
 #include "logo_device.cuh"
@@ -94,15 +96,50 @@ __device__ __forceinline__ void reverse2_f4(float4* T, uint32_t a0, uint32_t a1,
     }
 }
 
-template <int R, int TC, int NT>
+// Sum over the CTA (every thread returns the total).
+template <int NT>
+__device__ __forceinline__ unsigned long long cta_sum(unsigned long long v,
+                                                      unsigned long long* part) {
+    v = warp_sum_u64(v);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned long long t = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) t += part[w];
+    __syncthreads();
+    return t;
+}
+
+// Exact incoming edge of every position of the shared tour.
+template <int NT>
+__device__ __forceinline__ void recompute_edges(OrderedCity* Q, uint32_t n) {
+    for (uint32_t k = threadIdx.x; k < n; k += NT) {
+        const OrderedCity a = Q[k];
+        const OrderedCity b = Q[k == 0 ? n - 1 : k - 1];
+        Q[k].e = (float)exact_dist(b.x, b.y, a.x, a.y);
+    }
+    __syncthreads();
+}
+
+// ILS == false: one descent (the multi-kernel descent's bookkeeping).
+// ILS == true: a whole ILS call.  Every CTA keeps the best tour's city ids in
+// shared memory and runs the same length, accept/revert and kick on its own
+// copy (ILSGlobalSolverSequential.cpp:87-94, ILSGlobalSolver.cpp:37-48 and
+// the double bridge), so those steps need no grid barrier; the sweeps of
+// consecutive descents take the best-key slots by a running sweep count.
+template <int R, int TC, int NT, bool ILS>
 __global__ void __launch_bounds__(NT) coop_descent_kernel(CoopArgs A) {
     constexpr int kCoopThreads = NT;
     constexpr int kCoopWarps = NT / 32;
     extern __shared__ __align__(16) unsigned char coop_smem[];
     OrderedCity* Q = reinterpret_cast<OrderedCity*>(coop_smem);
     const uint32_t n = A.n;
+    constexpr uint32_t RT = 32 * R;
+    const uint32_t nrb = (n - 3 + RT - 1) / RT;  // row blocks over rows 1..n-3
     uint32_t* tbl = reinterpret_cast<uint32_t*>(coop_smem + (size_t)n * sizeof(OrderedCity));
+    uint32_t* sbest = tbl + (nrb + 2);  // ILS: city ids of the best tour
     __shared__ unsigned long long wbest[kCoopWarps];
+    __shared__ unsigned long long psum[kCoopWarps];
     __shared__ bool bar_ok;
     DevState* st = A.st;
     CoopSync* cs = A.cs;
@@ -115,9 +152,8 @@ __global__ void __launch_bounds__(NT) coop_descent_kernel(CoopArgs A) {
         OrderedCity o = Qg[k];
         o.pad = __uint_as_float(Rg[k]);
         Q[k] = o;
+        if (ILS) sbest[k] = A.route_best[k];
     }
-    constexpr uint32_t RT = 32 * R;
-    const uint32_t nrb = (n - 3 + RT - 1) / RT;  // row blocks over rows 1..n-3
     if (threadIdx.x == 0) {
         uint32_t acc = 0;
         tbl[0] = 0;
@@ -130,119 +166,184 @@ __global__ void __launch_bounds__(NT) coop_descent_kernel(CoopArgs A) {
     __syncthreads();
     const uint32_t total = tbl[nrb];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned long long m0 = *(volatile unsigned long long*)&st->moves;
+    unsigned long long m0 = *(volatile unsigned long long*)&st->moves;
     const unsigned long long maxm = *(volatile unsigned long long*)&st->max_moves;
-    unsigned long long m = 0, sweeps = 0;
+    unsigned long long m = 0, sweeps = 0, seq = 0, total_m = 0;
+    unsigned long long best_len = 0, accepted = 0, kicks = 0;
+    uint64_t rng = 0;
+    if (ILS) {
+        best_len = *(volatile unsigned long long*)&st->best_length;
+        rng = *(volatile unsigned long long*)&st->rng;
+    }
     bool limit = false, bad = false, failed = false;
-    for (;;) {
-        // sweep: warp tiles dealt over every warp of the grid
-        uint64_t best = kNoMove;
-        for (uint32_t t = blockIdx.x * kCoopWarps + warp; t < total;
-             t += gridDim.x * kCoopWarps) {
-            uint32_t lo = 0, hi = nrb;  // row block b with tbl[b] <= t < tbl[b + 1]
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) / 2;
-                if (tbl[mid] <= t) lo = mid; else hi = mid;
+    float4* T = reinterpret_cast<float4*>(Q);
+    for (uint32_t it = 0;; ++it) {
+        m = 0;
+        for (;;) {
+            // sweep: warp tiles dealt over every warp of the grid
+            uint64_t best = kNoMove;
+            for (uint32_t t = blockIdx.x * kCoopWarps + warp; t < total;
+                 t += gridDim.x * kCoopWarps) {
+                uint32_t lo = 0, hi = nrb;  // row block b with tbl[b] <= t < tbl[b + 1]
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (tbl[mid] <= t) lo = mid; else hi = mid;
+                }
+                const uint32_t row0 = 1 + lo * RT;
+                const uint32_t col0 = row0 + 2 + (t - tbl[lo]) * TC;
+                const uint32_t col1 = min(col0 + TC, n);
+                const uint32_t ib = row0 + lane * R;
+                int B = -1;
+                if (best != kNoMove) B = min(B, key_delta(best));
+                RowBlock<R> rb;
+                load_rows<R>(rb, Q, ib, n);
+                refresh_thresholds<R>(rb, Q, ib, n, B, A.margin);
+                walk_columns<R>(rb, Q, 0, col0, col1, ib, n, Q, A.margin, B, best);
             }
-            const uint32_t row0 = 1 + lo * RT;
-            const uint32_t col0 = row0 + 2 + (t - tbl[lo]) * TC;
-            const uint32_t col1 = min(col0 + TC, n);
-            const uint32_t ib = row0 + lane * R;
-            int B = -1;
-            if (best != kNoMove) B = min(B, key_delta(best));
-            RowBlock<R> rb;
-            load_rows<R>(rb, Q, ib, n);
-            refresh_thresholds<R>(rb, Q, ib, n, B, A.margin);
-            walk_columns<R>(rb, Q, 0, col0, col1, ib, n, Q, A.margin, B, best);
-        }
-        best = warp_min_u64(best);
-        if (lane == 0) wbest[warp] = best;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long k = wbest[0];
+            best = warp_min_u64(best);
+            if (lane == 0) wbest[warp] = best;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned long long k = wbest[0];
 #pragma unroll
-            for (int w = 1; w < kCoopWarps; ++w) k = wbest[w] < k ? wbest[w] : k;
-            if (k != kNoMove) atomicMin(&cs->slot[m % 3], k);
-            if (blockIdx.x == 0) cs->slot[(m + 1) % 3] = kNoMove;
-        }
-        if (!grid_barrier(cs, gridDim.x, st, &bar_ok)) {
-            failed = true;
-            break;
-        }
-        ++sweeps;
-        const unsigned long long key = ld_acquire_u64(&cs->slot[m % 3]);
-        if (key == kNoMove) break;  // local optimum
-        // reported move (i, j+1): p = i < q = j+1 (twoOptLocalSolver.cpp:41-48)
-        const uint32_t p = key_i(key), q = key_j(key);
-        if (!(p >= 1 && q < n && q >= p + 2)) {
-            bad = true;
-            break;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            int* log = st->move_log;
-            const unsigned long long idx = m0 + m;
-            if (log && idx < st->log_cap) {
-                log[3 * idx + 0] = key_delta(key);
-                log[3 * idx + 1] = (int)p;
-                log[3 * idx + 2] = (int)q;
+                for (int w = 1; w < kCoopWarps; ++w) k = wbest[w] < k ? wbest[w] : k;
+                if (k != kNoMove) atomicMin(&cs->slot[seq % 3], k);
+                if (blockIdx.x == 0) cs->slot[(seq + 1) % 3] = kNoMove;
+            }
+            if (!grid_barrier(cs, gridDim.x, st, &bar_ok)) {
+                failed = true;
+                break;
+            }
+            ++sweeps;
+            const unsigned long long key = ld_acquire_u64(&cs->slot[seq % 3]);
+            ++seq;
+            if (key == kNoMove) break;  // local optimum
+            // reported move (i, j+1): p = i < q = j+1 (twoOptLocalSolver.cpp:41-48)
+            const uint32_t p = key_i(key), q = key_j(key);
+            if (!(p >= 1 && q < n && q >= p + 2)) {
+                bad = true;
+                break;
+            }
+            if (!ILS && blockIdx.x == 0 && threadIdx.x == 0) {
+                int* log = st->move_log;
+                const unsigned long long idx = m0 + m;
+                if (log && idx < st->log_cap) {
+                    log[3 * idx + 0] = key_delta(key);
+                    log[3 * idx + 1] = (int)p;
+                    log[3 * idx + 2] = (int)q;
+                }
+            }
+            // new = old[p..q) ++ rev(old[0..p)) ++ rev(old[q..n))
+            reverse2_f4<NT>(T, p, q, q, n);
+            __syncthreads();
+            reverse2_f4<NT>(T, 0, q, 0, 0);
+            __syncthreads();
+            recompute_edges<NT>(Q, n);
+            ++m;
+            if (m0 + m >= maxm) {
+                limit = true;
+                break;
             }
         }
-        // new = old[p..q) ++ rev(old[0..p)) ++ rev(old[q..n))
-        float4* T = reinterpret_cast<float4*>(Q);
-        reverse2_f4<NT>(T, p, q, q, n);
-        __syncthreads();
-        reverse2_f4<NT>(T, 0, q, 0, 0);
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads) {
-            const OrderedCity a = Q[k];
-            const OrderedCity b = Q[k == 0 ? n - 1 : k - 1];
-            Q[k].e = (float)exact_dist(b.x, b.y, a.x, a.y);
+        total_m += m;
+        if (!ILS || failed || bad) break;
+        // length of this CTA's copy; keep it if strictly shorter, else revert
+        unsigned long long part = 0;
+        for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads)
+            part += (unsigned long long)Q[k].e;
+        const unsigned long long len = cta_sum<NT>(part, psum);
+        if (len < best_len) {
+            for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads)
+                sbest[k] = __float_as_uint(Q[k].pad);
+            best_len = len;
+            ++accepted;
+        } else {
+            for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads) {
+                const uint32_t id = sbest[k];
+                const float2 c = A.xy[id];
+                Q[k] = OrderedCity{c.x, c.y, 0.f, __uint_as_float(id)};
+            }
+            __syncthreads();
+            recompute_edges<NT>(Q, n);
         }
         __syncthreads();
-        ++m;
-        if (m0 + m >= maxm) {
-            limit = true;
-            break;
+        if (it == A.kicks) break;
+        // kick (the same draws as kick_kernel in tour.cu)
+        if (A.kick_kind == 1) {
+            uint32_t c[3];
+            for (int k = 0; k < 3; ++k) c[k] = 1 + uniform_below(rng, n - 1);
+            uint32_t t;
+            if (c[1] < c[0]) { t = c[0]; c[0] = c[1]; c[1] = t; }
+            if (c[2] < c[1]) { t = c[1]; c[1] = c[2]; c[2] = t; }
+            if (c[1] < c[0]) { t = c[0]; c[0] = c[1]; c[1] = t; }
+            // old[0,p1) old[p2,p3) old[p1,p2) old[p3,n): swap two adjacent blocks
+            reverse2_f4<NT>(T, c[0], c[1], c[1], c[2]);
+            __syncthreads();
+            reverse2_f4<NT>(T, c[0], c[2], 0, 0);
+        } else {
+            uint32_t a = uniform_below(rng, n);
+            uint32_t b = uniform_below(rng, n);
+            if (b < a) { const uint32_t t = a; a = b; b = t; }
+            // rotate by a, reverse [b - a, n): old[a,b) ++ rev(old[0,a)) ++ rev(old[b,n))
+            reverse2_f4<NT>(T, a, b, b, n);
+            __syncthreads();
+            reverse2_f4<NT>(T, 0, b, 0, 0);
         }
+        __syncthreads();
+        recompute_edges<NT>(Q, n);
+        ++kicks;
+        m0 = 0;
     }
     if (blockIdx.x == 0 && !failed) {
         for (uint32_t k = threadIdx.x; k < n; k += kCoopThreads) {
             OrderedCity o = Q[k];
-            Rg[k] = __float_as_uint(o.pad);
+            const uint32_t id = __float_as_uint(o.pad);
             o.pad = 0.f;
+            Rg[k] = id;
             Qg[k] = o;
+            if (ILS) {
+                A.route_best[k] = id;
+                A.Qbest[k] = o;
+            }
         }
         if (threadIdx.x == 0) {
             st->moves = m0 + m;
-            st->total_moves += m;
+            st->total_moves += total_m;
             st->sweeps += sweeps;
             st->best_key = kNoMove;
             st->converged = 1;
+            if (ILS) {
+                st->rng = rng;
+                st->best_length = best_len;
+                st->accepted += accepted;
+                st->kicks += kicks;
+            }
             if (limit) atomicOr(&st->status, kErrMoveLimit);
             if (bad) atomicOr(&st->status, kErrBadKey);
         }
     }
 }
 
-template <int R, int TC>
+template <int R, int TC, bool ILS>
 size_t coop_smem(uint32_t n) {
     const uint32_t nrb = (n - 3 + 32 * R - 1) / (32 * R);
-    return (size_t)n * sizeof(OrderedCity) + sizeof(uint32_t) * (nrb + 2);
+    return (size_t)n * sizeof(OrderedCity) + sizeof(uint32_t) * (nrb + 2) +
+           (ILS ? sizeof(uint32_t) * (size_t)n : 0);
 }
 
 // Grid for a cooperative launch: every CTA resident at once (occupancy x
 // SMs), and no more CTAs than the sweep has warp tiles for.
-template <int R, int TC, int NT>
+template <int R, int TC, int NT, bool ILS>
 int coop_grid_t(uint32_t n, uint32_t max_n, int device) {
-    const size_t smem = coop_smem<R, TC>(n);
+    const size_t smem = coop_smem<R, TC, ILS>(n);
     // the limit is shared by every context: set it for the largest n this
     // instantiation runs, not for this context's n
-    if (cudaFuncSetAttribute(coop_descent_kernel<R, TC, NT>,
+    if (cudaFuncSetAttribute(coop_descent_kernel<R, TC, NT, ILS>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)coop_smem<R, TC>(max_n)) != cudaSuccess)
+                             (int)coop_smem<R, TC, ILS>(max_n)) != cudaSuccess)
         return 0;
     int per_sm = 0, sms = 0, coop = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_descent_kernel<R, TC, NT>,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_descent_kernel<R, TC, NT, ILS>,
                                                       NT, smem) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess)
@@ -256,12 +357,13 @@ int coop_grid_t(uint32_t n, uint32_t max_n, int device) {
     return (int)(want < cap ? (want < 1 ? 1 : want) : cap);
 }
 
-template <int R, int TC, int NT>
+template <int R, int TC, int NT, bool ILS>
 cudaError_t launch_coop_t(const CoopArgs& A, int grid, cudaStream_t s) {
     CoopArgs a = A;
     void* args[] = {&a};
-    return cudaLaunchCooperativeKernel((const void*)coop_descent_kernel<R, TC, NT>, dim3(grid),
-                                       dim3(NT), args, coop_smem<R, TC>(A.n), s);
+    return cudaLaunchCooperativeKernel((const void*)coop_descent_kernel<R, TC, NT, ILS>,
+                                       dim3(grid), dim3(NT), args,
+                                       coop_smem<R, TC, ILS>(A.n), s);
 }
 
 // Test hook for the bounded wait: one CTA waits at a barrier sized for two,
@@ -287,13 +389,24 @@ cudaError_t launch_barrier_probe(CoopSync* cs, DevState* st, cudaStream_t s) {
 // descent is as fast or faster, so the limit is 6,144).
 int coop_grid(uint32_t n, int device) {
     if (n < 8 || n > kCoopMaxN) return 0;
-    return n <= kCoopSmallN ? coop_grid_t<2, 32, 256>(n, kCoopSmallN, device)
-                            : coop_grid_t<2, 32, 512>(n, kCoopMaxN, device);
+    return n <= kCoopSmallN ? coop_grid_t<2, 32, 256, false>(n, kCoopSmallN, device)
+                            : coop_grid_t<2, 32, 512, false>(n, kCoopMaxN, device);
+}
+
+int coop_ils_grid(uint32_t n, int device) {
+    if (n < 8 || n > kCoopMaxN) return 0;
+    return n <= kCoopSmallN ? coop_grid_t<2, 32, 256, true>(n, kCoopSmallN, device)
+                            : coop_grid_t<2, 32, 512, true>(n, kCoopMaxN, device);
 }
 
 cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s) {
-    return A.n <= kCoopSmallN ? launch_coop_t<2, 32, 256>(A, grid, s)
-                              : launch_coop_t<2, 32, 512>(A, grid, s);
+    return A.n <= kCoopSmallN ? launch_coop_t<2, 32, 256, false>(A, grid, s)
+                              : launch_coop_t<2, 32, 512, false>(A, grid, s);
+}
+
+cudaError_t launch_coop_ils(const CoopArgs& A, int grid, cudaStream_t s) {
+    return A.n <= kCoopSmallN ? launch_coop_t<2, 32, 256, true>(A, grid, s)
+                              : launch_coop_t<2, 32, 512, true>(A, grid, s);
 }
 
 }  // namespace logo

@@ -61,6 +61,13 @@ struct DevState {
     unsigned int bad_route;         // set by the gather: the route is not a permutation
     int* move_log;                  // (delta, i, j) per move, or null
     unsigned long long length_acc;  // partial sums of tour_length_kernel
+    // ILS run on the device (one graph or one cooperative launch per call)
+    unsigned long long kick_target; // kicks to apply in this call
+    unsigned long long loop_mark;   // moves at the previous descent-loop check
+    unsigned long long ils_iters;   // kick-loop passes so far (guard)
+    unsigned long long start_length; // length of the tour the call started from
+    unsigned int kick_kind;         // LOGO_KICK_SEGMENT or LOGO_KICK_DOUBLE_BRIDGE
+    unsigned int ils_pad;
 };
 
 __host__ __device__ __forceinline__ uint64_t pack_key(int delta, uint32_t i,

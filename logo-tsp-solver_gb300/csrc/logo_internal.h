@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/logo_gpu.h"
 #include "logo_device.cuh"
 
 namespace logo {
@@ -17,7 +18,7 @@ struct SweepLaunch {
     uint32_t ntiles;
     uint32_t cb;         // columns per tile
     int R, NW;           // rows per thread, warps per CTA
-    int variant;         // LOGO_SWEEP_* (0 MUFU, 1 MUFU f32x2, 2 squared, 3 squared f32x2, 4 fused, 5 local, 6 boxed)
+    int variant;         // LOGO_SWEEP_* (0 MUFU, 4 fused, 5 local, 6 boxed; 1-3 retired)
     float margin;        // filter margin M
     DevState* st;
     // boxed variant (6): per 32-column window (columns 3 + 32g ..) its coordinate
@@ -31,7 +32,17 @@ struct SweepLaunch {
     float* rmax;
     uint4* work;
     uint32_t* workctl;
+    // boxed variant: the tour's city ids (both buffers), the tour position of
+    // every city (written by the window pass) and kSeedNeighbours nearest
+    // neighbours per city, whose pairs seed the sweep's best delta
+    const uint32_t* R0;
+    const uint32_t* R1;
+    uint32_t* pos;
+    const uint32_t* nbr;
 };
+constexpr uint32_t kSeedNeighbours = 5;
+// k nearest other cities of every city, out[v * k + j] (construct.cpp).
+void knn_grid(const ::logo_xy* p, uint32_t n, uint32_t k, uint32_t* out);
 // Windows of the boxed variant: columns 3 + 32 g .. 3 + 32 g + 31 (< n) and
 // rows 1 + 32 g .. 1 + 32 g + 31 (rows with pairs: i + 3 <= n).
 __host__ __device__ inline uint32_t sweep_windows(uint32_t n) {
@@ -79,10 +90,23 @@ struct CoopArgs {
     float margin;
     DevState* st;
     CoopSync* cs;  // count = gen = 0 and every slot = kNoMove before the launch
+    // ILS launch only: coordinates by city id, the best tour (also the start:
+    // route_best/Qbest and st->best_length are set before the launch) and the
+    // kick count and kind
+    const float2* xy;
+    OrderedCity* Qbest;
+    uint32_t* route_best;
+    uint32_t kicks;
+    int kick_kind;
 };
-// CTAs for a cooperative launch at this n on `device` (0: not available).
+// CTAs for a cooperative launch at this n on `device` (0: not available);
+// coop_ils_grid for the launch that runs a whole ILS call.
 int coop_grid(uint32_t n, int device);
+int coop_ils_grid(uint32_t n, int device);
 cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s);
+// One cooperative launch runs descent, length, accept/revert and kicks for
+// A.kicks kicks (ILSGlobalSolverSequential::optimize with a kick count).
+cudaError_t launch_coop_ils(const CoopArgs& A, int grid, cudaStream_t s);
 // One CTA waits at the cooperative grid barrier sized for two (test hook).
 cudaError_t launch_barrier_probe(CoopSync* cs, DevState* st, cudaStream_t s);
 
@@ -103,6 +127,13 @@ cudaError_t launch_tour_length(const TourBufs& T, cudaStream_t s);
 cudaError_t launch_kick(const TourBufs& T, int kind, cudaStream_t s);
 cudaError_t launch_accept(const TourBufs& T, cudaStream_t s);
 cudaError_t launch_save_best(const TourBufs& T, cudaStream_t s);
+// Kick of the kind in st->kick_kind.
+inline cudaError_t launch_kick_dev(const TourBufs& T, cudaStream_t s) { return launch_kick(T, -1, s); }
+// Set the WHILE conditions of the device-run ILS graph (see tour.cu).
+cudaError_t launch_descent_cond(DevState* st, cudaGraphConditionalHandle h, bool first,
+                                cudaStream_t s);
+cudaError_t launch_kick_cond(DevState* st, cudaGraphConditionalHandle h, bool first,
+                             cudaStream_t s);
 
 // Upper bound of |exact delta - approximate delta| for coordinates whose
 // bounding-box diagonal is `diag` (see filter_margin in capi.cu).

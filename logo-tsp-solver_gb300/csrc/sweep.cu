@@ -276,15 +276,21 @@ __device__ __forceinline__ void window_reduce(float& m, float& x0, float& x1, fl
 
 __global__ void __launch_bounds__(256)
     window_stats_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                        uint32_t n, float4* __restrict__ wbox, float* __restrict__ wmax,
-                        float4* __restrict__ rbox, float* __restrict__ rmax,
-                        uint32_t* __restrict__ workctl, DevState* st) {
+                        const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
+                        uint32_t* __restrict__ pos, uint32_t n, float4* __restrict__ wbox,
+                        float* __restrict__ wmax, float4* __restrict__ rbox,
+                        float* __restrict__ rmax, uint32_t* __restrict__ workctl, DevState* st) {
     if (*(volatile unsigned int*)&st->converged) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         workctl[0] = 0u;
         workctl[1] = 0u;
     }
-    const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
+    const bool cur = *(volatile unsigned int*)&st->cur;
+    const OrderedCity* Q = cur ? Q1 : Q0;
+    // tour position of every city, for the seed pass
+    const uint32_t* R = cur ? R1 : R0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        pos[min(R[k], n - 1)] = k;
     const uint32_t g = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (g < sweep_windows(n)) {  // whole warps
         const uint32_t c = 3 + g * kWin6 + lane;
@@ -314,14 +320,82 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Boxed variant, seed pass: for every tour position i and each of the
+// kSeedNeighbours nearest neighbours v of its city (at position p = pos[v]),
+// the two pairs whose move creates the short edge (i, p): (a, b) =
+// (min, max) of (i, p), whose delta has d(a, b) = d(i, p) as its first term,
+// and (a + 1, b + 1), which has it as its second.  Their exact deltas are
+// real pairs of this sweep, so the best of them is a valid starting bound:
+// the sweep's best delta is at most that, and the tile filter and the boxed
+// kernel prune with it from the start instead of with -1.  The lowest key
+// goes to st->best_key, where it competes with every other pair, so the
+// chosen move is still the exact lowest (delta, i, c).
+__global__ void __launch_bounds__(256)
+    seed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
+                const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
+                const uint32_t* __restrict__ pos, const uint32_t* __restrict__ nbr, uint32_t n,
+                DevState* st) {
+    constexpr uint32_t K = kSeedNeighbours;
+    if (*(volatile unsigned int*)&st->converged) return;
+    const bool cur = *(volatile unsigned int*)&st->cur;
+    const OrderedCity* Q = cur ? Q1 : Q0;
+    const uint32_t* R = cur ? R1 : R0;
+    uint64_t best = kNoMove;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        // every load of a position's candidates is issued before any is used
+        const uint32_t t = min(R[i], n - 1);
+        const OrderedCity qi = Q[i], qim = Q[i >= 1 ? i - 1 : 0], qip = Q[min(i + 1, n - 1)];
+        uint32_t p[K];
+#pragma unroll
+        for (uint32_t k = 0; k < K; ++k) p[k] = nbr[(size_t)t * K + k];
+#pragma unroll
+        for (uint32_t k = 0; k < K; ++k) p[k] = min(pos[min(p[k], n - 1)], n - 1);
+        OrderedCity qp[K], qpm[K], qpp[K];
+#pragma unroll
+        for (uint32_t k = 0; k < K; ++k) {
+            qp[k] = Q[p[k]];
+            qpm[k] = Q[p[k] >= 1 ? p[k] - 1 : 0];
+            qpp[k] = Q[min(p[k] + 1, n - 1)];
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < K; ++k) {
+            const uint32_t a = min(i, p[k]), b = max(i, p[k]);
+            if (b < a + 2) continue;  // also p == i
+            const int D = exact_dist(qi.x, qi.y, qp[k].x, qp[k].y);
+            const int ee = (int)qi.e + (int)qp[k].e;
+            if (a >= 1) {
+                // pair (a, b): d(a, b) + d(a - 1, b - 1) - e[a] - e[b]
+                const int delta = D + exact_dist(qim.x, qim.y, qpm[k].x, qpm[k].y) - ee;
+                if (delta < 0) {
+                    const uint64_t key = pack_key(delta, a, b);
+                    best = key < best ? key : best;
+                }
+            }
+            if (b + 1 <= n - 1) {
+                // pair (a + 1, b + 1): d(a + 1, b + 1) + d(a, b) - e[a + 1] - e[b + 1]
+                const int delta = exact_dist(qip.x, qip.y, qpp[k].x, qpp[k].y) + D -
+                                  (int)qip.e - (int)qpp[k].e;
+                if (delta < 0) {
+                    const uint64_t key = pack_key(delta, a + 1, b + 1);
+                    best = key < best ? key : best;
+                }
+            }
+        }
+    }
+    best = warp_min_u64(best);
+    if ((threadIdx.x & 31) == 0 && best != kNoMove)
+        atomicMin(&st->best_key, (unsigned long long)best);
+}
+
 // Boxed variant, pass 2: gridDim.y CTAs per row block (the rows of one tile
 // row, rows_per_tile of them from row0 = 1 + rows_per_tile * blockIdx.x).
 // The block's row-window statistics go to shared memory; each warp then
 // takes 32 consecutive column windows of the block at a time (lane = column
 // window, 32 / (cb / 32) tiles per step; the CTAs of a row block split its
-// steps) and tests them against every row window with B = -1, the largest best delta a sweep can end with
-// (box_gap_pass with u = -1 + E_r + 5 + E_c, which bounds every V + 5 of
-// those pairs).  Tiles with a passing pair are appended to the work list as
+// steps) and tests them against every row window with B = the seed pass's
+// best delta, or -1 (the largest best delta a sweep can end with) if it
+// found none (box_gap_pass with u = B + E_r + 5 + E_c, which bounds every
+// V + 5 of those pairs).  Tiles with a passing pair are appended to the work list as
 // (row0, col0, mask of their column windows that passed).  The tiles are
 // the ones the tile list holds: columns from row0 + 2 to n - 1 in steps of
 // cb.
@@ -333,6 +407,13 @@ __global__ void __launch_bounds__(256)
     __shared__ float4 srb[kMaxTileRows / kWin6];
     __shared__ float sre[kMaxTileRows / kWin6];
     if (*(volatile unsigned int*)&st->converged) return;
+    // B: the seed pass's best delta (a real pair of this sweep), else -1
+    int B = -1;
+    {
+        const uint64_t gk = *(volatile unsigned long long*)&st->best_key;
+        if (gk != kNoMove) B = min(B, key_delta(gk));
+    }
+    const float b5 = (float)(B + 5);
     const uint32_t row0 = 1 + blockIdx.x * rows_per_tile;
     const uint32_t ntiles = (n - row0 - 2 + cb - 1) / cb;  // columns row0 + 2 .. n - 1
     const uint32_t wpt = cb / kWin6;                       // windows per tile (cb % 32 == 0)
@@ -341,12 +422,31 @@ __global__ void __launch_bounds__(256)
     const uint32_t row_end = min(row0 + rows_per_tile, n - 2);  // rows i + 3 <= n
     const uint32_t nrw = (row_end - row0 + kWin6 - 1) / kWin6;
     const uint32_t rw0 = (row0 - 1) / kWin6;
+    __shared__ float4 sub;  // the whole row block: union of its row windows' boxes
+    __shared__ float sue;   // and their largest edge
     for (uint32_t r = threadIdx.x; r < nrw; r += blockDim.x) {
         srb[r] = rbox[rw0 + r];
         sre[r] = rmax[rw0 + r];
     }
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        float m = -3.0e7f, x0 = FLT_MAX, x1 = -FLT_MAX, y0 = FLT_MAX, y1 = -FLT_MAX;
+        for (uint32_t r = lane; r < nrw; r += 32) {
+            const float4 b = srb[r];
+            m = fmaxf(m, sre[r]);
+            x0 = fminf(x0, b.x);
+            x1 = fmaxf(x1, b.y);
+            y0 = fminf(y0, b.z);
+            y1 = fmaxf(y1, b.w);
+        }
+        window_reduce(m, x0, x1, y0, y1);
+        if (lane == 0) {
+            sub = make_float4(x0, x1, y0, y1);
+            sue = m;
+        }
+    }
+    __syncthreads();
     const uint32_t col_start = row0 + 2;
     for (uint32_t t0 = (blockIdx.y * 8 + warp) * tps; t0 < ntiles; t0 += gridDim.y * 8 * tps) {
         const uint32_t tk = t0 + lane / wpt;
@@ -357,9 +457,11 @@ __global__ void __launch_bounds__(256)
             const float4 cbx = wbox[cw];
             const float ce = wmax[cw];
             const uint32_t last_col = min(col + kWin6, n) - 1;
-            for (uint32_t r = 0; r < nrw; ++r) {
+            // the block test first: no row window passes unless the union does
+            const bool block = box_gap_pass(sub, cbx, (sue + b5) + ce);
+            for (uint32_t r = 0; block && r < nrw; ++r) {
                 if (last_col < row0 + r * kWin6 + 2) break;  // no pair c >= i + 2 from here on
-                if (box_gap_pass(srb[r], cbx, (sre[r] + 4.f) + ce)) {
+                if (box_gap_pass(srb[r], cbx, (sre[r] + b5) + ce)) {
                     any = true;
                     break;
                 }
@@ -644,8 +746,8 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
     return cudaGetLastError();
 }
 
-// Boxed variant: window statistics, tile filter, persistent sweep (one CTA
-// per resident slot).
+// Boxed variant: window statistics (and city positions), near-neighbour
+// seed, tile filter, persistent sweep (one CTA per resident slot).
 template <int R, int NW>
 static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     const size_t smem = boxed_smem_bytes(L.cb, NW);
@@ -673,8 +775,10 @@ static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool pre
     }
     const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
     const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
-    window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.n, L.wbox, L.wmax, L.rbox,
-                                                       L.rmax, L.workctl, L.st);
+    window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.n, L.wbox,
+                                                       L.wmax, L.rbox, L.rmax, L.workctl, L.st);
+    const uint32_t sgrid = (L.n + 255) / 256 < 4096 ? (L.n + 255) / 256 : 4096;
+    seed_kernel<<<sgrid, 256, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.nbr, L.n, L.st);
     const uint32_t rows_per_tile = (uint32_t)(NW * 32 * R);
     const uint32_t row_blocks = (L.n - 4) / rows_per_tile + 1;  // row0 + 3 <= n
     // CTAs per row block: one step per warp for the longest row (block 0)

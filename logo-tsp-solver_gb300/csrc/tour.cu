@@ -168,8 +168,10 @@ __global__ void tour_length_kernel(TourBufs T) {
     }
 }
 
+// kind < 0: the kind stored in st->kick_kind (the device-run ILS graph).
 __global__ void kick_kernel(TourBufs T, int kind) {
     DevState* st = T.st;
+    if (kind < 0) kind = (int)*(volatile unsigned int*)&st->kick_kind;
     const uint32_t cur = *(volatile unsigned int*)&st->cur;
     uint64_t rng = *(volatile unsigned long long*)&st->rng;
     const uint32_t n = T.n;
@@ -236,10 +238,57 @@ __global__ void save_best_kernel(TourBufs T) {
         T.Qbest[k] = (cur ? T.Q[1] : T.Q[0])[k];
         T.route_best[k] = (cur ? T.route[1] : T.route[0])[k];
     }
-    if (last_block_done(&st->done_blocks)) st->best_length = st->length;
+    if (last_block_done(&st->done_blocks)) {
+        st->best_length = st->length;
+        st->start_length = st->length;
+    }
+}
+
+// Loop conditions of the device-run ILS graph (one thread each).  The
+// descent loop runs while the tour has not converged and no error bit other
+// than the move limit is set; every pass of its body applies at least one
+// move or converges, so a pass that did neither stops the loop with
+// kErrInternal.  Neither loop runs on a route that failed the permutation
+// check.  The kick loop runs while fewer than kick_target kicks have
+// been applied; each pass applies exactly one, so more passes than
+// kick_target stop it with kErrInternal.  `first` marks the check in front
+// of a loop (it resets the guard).
+__global__ void descent_cond_kernel(DevState* st, cudaGraphConditionalHandle h, int first) {
+    const unsigned int bad = (st->status & ~kErrMoveLimit) | st->bad_route;
+    bool go = !st->converged && !bad;
+    if (!first && go && st->moves == st->loop_mark) {
+        atomicOr(&st->status, kErrInternal);
+        go = false;
+    }
+    st->loop_mark = st->moves;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+__global__ void kick_cond_kernel(DevState* st, cudaGraphConditionalHandle h, int first) {
+    const unsigned int bad = (st->status & ~kErrMoveLimit) | st->bad_route;
+    bool go = st->kicks < st->kick_target && !bad;
+    if (first) {
+        st->ils_iters = 0;
+    } else if (++st->ils_iters > st->kick_target) {
+        atomicOr(&st->status, kErrInternal);
+        go = false;
+    }
+    cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
 }  // namespace
+
+cudaError_t launch_descent_cond(DevState* st, cudaGraphConditionalHandle h, bool first,
+                                cudaStream_t s) {
+    descent_cond_kernel<<<1, 1, 0, s>>>(st, h, first ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kick_cond(DevState* st, cudaGraphConditionalHandle h, bool first,
+                             cudaStream_t s) {
+    kick_cond_kernel<<<1, 1, 0, s>>>(st, h, first ? 1 : 0);
+    return cudaGetLastError();
+}
 
 // Clears the permutation check before launch_init_ordered: the seen bitmap,
 // the bad-route flag and the current-buffer index (one launch instead of

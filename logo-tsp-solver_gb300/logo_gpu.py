@@ -50,6 +50,7 @@ EXPORTS = [
     "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
     "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
     "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
+    "logo_diag_flag_timeout",
 ]
 
 
@@ -81,7 +82,7 @@ class CtxInfo(ctypes.Structure):
                 ("tile_cols", ctypes.c_uint32), ("tiles", ctypes.c_uint32),
                 ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32),
                 ("variant", ctypes.c_int), ("descent_mode", ctypes.c_int),
-                ("cooperative_ctas", ctypes.c_int)]
+                ("cooperative_ctas", ctypes.c_int), ("host_waits", ctypes.c_uint64)]
 
 
 class Instance(ctypes.Structure):
@@ -177,6 +178,7 @@ def load(path=LIB_PATH):
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
                                      c.c_uint64, c.POINTER(Stats)]
     L.logo_diag_sqrt_error.argtypes = [c.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.logo_diag_flag_timeout.argtypes = [_vp]
     L.logo_diag_wait_limits.argtypes = [c.c_int, ctypes.POINTER(ctypes.c_uint32),
                                         ctypes.POINTER(ctypes.c_uint32),
                                         ctypes.POINTER(ctypes.c_double)]
@@ -372,6 +374,11 @@ class Solver:
     @property
     def stream(self):
         return load().logo_ctx_stream(self._h)
+
+    def flag_timeout(self):
+        """Test hook: marks the context's device status as a timed-out wait
+        would (logo_diag_flag_timeout)."""
+        _check(load().logo_diag_flag_timeout(self._h), self._h)
 
 
 def read_tsplib(path):

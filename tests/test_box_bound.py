@@ -87,11 +87,23 @@ def test_box_test_keeps_every_choosable_block(inst, B, rows):
     assert checked > 0 and closed > 0  # the test was exercised both ways
 
 
-def test_tile_filter_bound_keeps_every_choosable_block(inst):
-    """The filter's form: 32-row windows against 32-column windows with B = -1
-    and u = E_r + 4 + E_c (largest incoming edges of the two windows)."""
+@pytest.mark.parametrize("bsel", ["minus_one", "true_best", "true_best_plus_7"])
+def test_tile_filter_bound_keeps_every_choosable_block(inst, oracle_mod, bsel):
+    """The filter's form: 32-row windows against 32-column windows with
+    u = B + 5 + E_r + E_c (largest incoming edges of the two windows), B = -1
+    or the seed pass's bound.  A seed is a real pair's delta, so it is never
+    below the sweep's best delta; the tightest B a seed can give is that best
+    delta itself, checked here together with a looser one.  Also the filter's
+    block test (the union of a row block's windows) in front of the
+    per-window tests: it must pass wherever one of its windows passes."""
     checked = 0
     for name, xy, route in _instances(inst):
+        B = -1
+        if bsel != "minus_one":
+            d, _, _ = oracle_mod.best_move(xy, route)
+            if d == 0:
+                continue
+            B = min(-1, d + (7 if bsel == "true_best_plus_7" else 0))
         q = xy[route].astype(F)
         n = len(q)
         x, y = q[:, 0], q[:, 1]
@@ -106,12 +118,20 @@ def test_tile_filter_bound_keeps_every_choosable_block(inst):
         rws = 1 + np.arange(nrw * 32).reshape(nrw, 32)
         rbox = np.stack([x[rws].min(1), x[rws].max(1), y[rws].min(1), y[rws].max(1)], -1)
         rmax = e[rws].max(1)
-        u = (rmax[:, None] + 4 + wmax[None, :]).astype(np.float64)
+        u = ((rmax[:, None] + F(B + 5)).astype(F) + wmax[None, :]).astype(np.float64)
         keep = _box_pass(rbox[:, None, :], wbox[None, :, :], u)
+        # row blocks of 16 windows (512 rows): union box and largest edge
+        for b0 in range(0, nrw, 16):
+            blk = slice(b0, min(b0 + 16, nrw))
+            ubox = np.array([rbox[blk, 0].min(), rbox[blk, 1].max(), rbox[blk, 2].min(),
+                             rbox[blk, 3].max()], F)
+            uu = ((F(rmax[blk].max()) + F(B + 5)).astype(F) + wmax).astype(np.float64)
+            ukeep = _box_pass(ubox[None, :], wbox, uu)
+            assert not (keep[blk].any(axis=0) & ~ukeep).any(), (name, b0)
         for r in range(nrw):
             ri = rws[r]
             d1 = _nint(x[ri][:, None, None], y[ri][:, None, None], x[cols][None], y[cols][None])
-            V = -1 + e[ri][:, None, None] + e[cols][None]
+            V = B + e[ri][:, None, None] + e[cols][None]
             ok = (d1 <= V) & (cols[None] >= ri[:, None, None] + 2)
             need = ok.any(axis=(0, 2))
             assert not (need & ~keep[r]).any(), (name, r, np.nonzero(need & ~keep[r]))

@@ -166,8 +166,11 @@ def test_descent_move_sequence_plain_workload(lg, inst, oracle_mod, seed, mode):
 
 @pytest.mark.parametrize("mode", ["graph", "cooperative"])
 @pytest.mark.parametrize("n,kicks,kind", [(200, 40, 0), (200, 40, 1), (523, 25, 0),
-                                          (523, 25, 1), (1500, 6, 1)])
+                                          (523, 25, 1), (1500, 6, 1), (300, 0, 0),
+                                          (3100, 8, 0), (3100, 8, 1)])
 def test_ils_matches_oracle(lg, inst, oracle_mod, n, kicks, kind, mode):
+    """The whole ILS call runs on the device: one cooperative launch, or one
+    graph whose descent and kick loops are conditional WHILE nodes."""
     xy = inst.uniform_f32(n, n, 1.0e4)
     r = inst.random_tour(n, n + 1)
     want, ost = oracle_mod.ils(xy, r, kicks, 1234 + n, kind)
@@ -180,6 +183,28 @@ def test_ils_matches_oracle(lg, inst, oracle_mod, n, kicks, kind, mode):
     assert st["moves"] == ost["moves"]
     assert st["accepted"] == ost["accepted"]
     assert st["kicks"] == kicks
+
+
+@pytest.mark.parametrize("mode", ["graph", "cooperative"])
+def test_ils_waits_on_the_device_a_fixed_number_of_times(lg, inst, oracle_mod, mode):
+    """An ILS call synchronises with the device a fixed number of times (the
+    state read, the tour download, the timer), however many kicks it runs, on
+    the cooperative launch and on the conditional graph."""
+    n = 1200
+    xy = inst.uniform_f32(n, 71, 1.0e4)
+    r = inst.random_tour(n, 72)
+    with lg.Solver(xy) as s:
+        s.set_descent_mode(lg.DESCENT_GRAPH if mode == "graph" else lg.DESCENT_COOPERATIVE)
+        waits = []
+        for kicks in (2, 60):
+            w0 = s.info()["host_waits"]
+            got, st = s.ils(r, kicks, 5, lg.KICK_DOUBLE_BRIDGE)
+            waits.append(s.info()["host_waits"] - w0)
+            assert st["kicks"] == kicks
+        want, ost = oracle_mod.ils(xy, r, 60, 5, lg.KICK_DOUBLE_BRIDGE,
+                                   threads=os.cpu_count() or 4)
+    assert np.array_equal(got, want) and st["final_length"] == ost["best_length"]
+    assert waits[0] == waits[1] and waits[1] <= 4, waits
 
 
 @pytest.mark.parametrize("n", [8, 2501, 6144])
@@ -285,13 +310,22 @@ def test_degenerate_instances(lg, inst, oracle_mod):
         assert np.array_equal(got, want)
 
 
-def test_small_n_has_no_move(lg, inst):
-    for n in (3, 4):
-        xy = inst.uniform_int(n, 1)
+def test_three_and_four_city_tours(lg, inst, oracle_mod):
+    """n = 3 has no pair; n = 4 has exactly one, (1, 2) reported as (1, 3),
+    which the reference's loop evaluates (src/solvers/cpuSolver.cpp:104,123)."""
+    xy = inst.uniform_int(3, 1)
+    with lg.Solver(xy) as s:
+        assert s.optimize_step(np.arange(3)) == (0, 0, 0)
+        got, st = s.optimize(np.arange(3))
+        assert st["moves"] == 0 and np.array_equal(got, np.arange(3))
+    for seed in range(1, 6):
+        xy = inst.uniform_int(4, seed)
+        r = inst.random_tour(4, seed)
         with lg.Solver(xy) as s:
-            assert s.optimize_step(np.arange(n)) == (0, 0, 0)
-            got, st = s.optimize(np.arange(n))
-            assert st["moves"] == 0 and np.array_equal(got, np.arange(n))
+            assert s.optimize_step(r) == oracle_mod.best_move(xy, r), seed
+            got, st = s.optimize(r)
+        want, m, _ = oracle_mod.descend(xy, r)
+        assert np.array_equal(got, want) and st["moves"] == m
 
 
 def test_invalid_arguments(lg, inst):
@@ -375,6 +409,29 @@ def test_device_waits_give_up_then_context_usable(lg, inst, oracle_mod):
     assert np.array_equal(got, want) and st["moves"] == 5
 
 
+def test_timed_out_context_is_not_used_again(lg, inst, oracle_mod):
+    """A device wait that gives up may leave a copy in flight, so its context
+    refuses every later call.  The timeout bit is set by a test hook (no wait
+    runs out here): the call that reads it returns TIMEOUT, every call after
+    it DEVICE_FAULT, and a new context on the same device works."""
+    xy = _instance(inst, 300, 6)
+    r = inst.random_tour(300, 106)
+    with lg.Solver(xy) as s:
+        s.set_route(r)
+        s.flag_timeout()
+        with pytest.raises(lg.LogoError) as e:
+            s.progress()
+        assert e.value.status == 4
+        for call in (lambda: s.optimize_step(r), lambda: s.optimize(r),
+                     lambda: s.ils(r, 2, 1, lg.KICK_SEGMENT), lambda: s.route_length(r),
+                     s.get_route, lambda: s.set_route(r), s.sweep_resident):
+            with pytest.raises(lg.LogoError) as e:
+                call()
+            assert e.value.status == 5
+    with lg.Solver(xy) as s:
+        assert s.optimize_step(r) == oracle_mod.best_move(xy, r)
+
+
 GROUPED_KERNELS = [(4, 4, 4, 256), (4, 4, 2, 256), (4, 4, 8, 128), (4, 8, 4, 512), (4, 8, 8, 256),
                    (4, 16, 4, 1024), (5, 4, 4, 256), (5, 4, 2, 256), (5, 4, 8, 128),
                    (5, 8, 4, 512), (5, 8, 8, 256), (5, 16, 4, 1024), (6, 4, 4, 256),
@@ -447,6 +504,34 @@ def test_full_descent_same_tour_every_large_variant(lg, inst, n, seed):
     for kernel, got, m, length in out[1:]:
         assert np.array_equal(got, out[0][1]), kernel
         assert (m, length) == (out[0][2], out[0][3]), kernel
+
+
+@pytest.mark.parametrize("n,grid", [(3000, 8), (600, 3), (20000, 64)])
+def test_boxed_seed_with_duplicate_points(lg, inst, oracle_mod, n, grid):
+    """The boxed sweep seeds its bound from near-neighbour pairs; with many
+    coincident cities (coordinates on a small integer grid) the neighbour
+    lists are full of ties and zero distances.  Single steps and a short
+    descent still equal the oracle's."""
+    rng = np.random.default_rng(n)
+    xy = (np.floor(rng.random((n, 2)) * grid) * 1000.0).astype(np.float32)
+    r = inst.random_tour(n, n + 3)
+    threads = os.cpu_count() or 4
+
+    def move(route):
+        key = oracle_mod.best_move_key(xy, route, threads=threads)
+        return (0, 0, 0) if key == (1 << 64) - 1 else oracle_mod.unpack_key(key)
+
+    with lg.Solver(xy) as s:
+        s.set_kernel(lg.SWEEP_BOXED, 4, 4, 128)
+        assert s.optimize_step(r) == move(r)
+        got, st = s.optimize(r, max_moves=30)
+    want = r.copy()
+    for _ in range(30):
+        d, i, j = move(want)
+        if d == 0:
+            break
+        want = oracle_mod.apply_move(want, i, j)
+    assert np.array_equal(got, want)
 
 
 def test_retired_variants_rejected(lg, inst):

@@ -362,8 +362,8 @@ def run_ours(a, world, rank, local, dist):
     roof.update({
         "kernel": ("logo::window_stats_kernel + logo::seed_kernel + logo::tile_filter_kernel + "
                    if SWEEP_LAUNCHES.get(info["variant"]) else "")
-                  + f"logo::{kname}<{info['rows_per_thread']},{info['warps_per_cta']}> "
-                  f"({screen}, {info['tile_cols']}-column tiles; timed together)",
+                  + f"logo::{kname}<{info['rows_per_thread']},{info['warps_per_cta']}>"
+                  + f" ({screen}, {info['tile_cols']}-column tiles; timed together)",
         "sweep_ms_mean": round(statistics.mean(sweep_ms), 4),
         "peak_source": f"152 SMs x 128 FP32/INT32 lanes x sm_max_mhz={sm_max:g} "
                        "(MEASURED_PEAKS.json)",

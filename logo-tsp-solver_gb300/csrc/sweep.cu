@@ -110,7 +110,8 @@ __host__ __device__ constexpr size_t sweep5_wmax_offset(uint32_t cb) {
 template <int R, int NW, int G>
 __global__ void __launch_bounds__(NW * 32)
     sweep_kernel5(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, DevState* st) {
+                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, float margin,
+                  DevState* st) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(NW * 32)
     }
     bs.G = bs.B;
     bs.busy = false;
+    bs.M = margin;
     RowBlock5<R> rb;
     load_rows5<R>(rb, Q, ib, n);
     refresh5<R>(rb, Q, ib, n, bs.B);
@@ -186,7 +188,8 @@ __host__ __device__ constexpr size_t sweep6_wmax_offset(uint32_t cb) {
 template <int R, int NW, int G>
 __global__ void __launch_bounds__(NW * 32)
     sweep_kernel6(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, DevState* st) {
+                  uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, float margin,
+                  DevState* st) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
@@ -223,6 +226,7 @@ __global__ void __launch_bounds__(NW * 32)
     }
     bs.G = bs.B;
     bs.busy = false;
+    bs.M = margin;
     const OrderedCity origin = Q[row0];  // same for every thread of the tile
     RowBlock6<R> rb;
     load_rows6<R>(rb, Q, ib, n, origin.x, origin.y);
@@ -540,7 +544,7 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
     sweep_boxed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                        uint32_t n, uint32_t cb, const float4* __restrict__ gbox,
                        const float* __restrict__ gmax, const uint4* __restrict__ work,
-                       uint32_t* __restrict__ workctl, DevState* st) {
+                       float margin, uint32_t* __restrict__ workctl, DevState* st) {
     static_assert(R <= 16 && NW * 32 <= 256, "unit encoding: 8-bit thread, 16-bit rows");
     constexpr int G = (128 / R) < 32 ? (128 / R) : 32;
     extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -570,6 +574,7 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
         if (gk != kNoMove) bs.B = min(bs.B, key_delta(gk));
     }
     bs.G = bs.B;
+    bs.M = margin;
     uint32_t parity = 0;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -671,7 +676,8 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
                     const uint32_t e = queue[u];
                     const uint32_t uib = row0 + (e >> 24) * R, w = (e >> 16) & 0xffu;
                     const uint32_t c = col0 + w * kWin7 + lane;
-                    if (c < col_end) unit7<R>(Q, stage, col0, c, uib, e & 0xffffu, n, bs.B, bs.best);
+                    if (c < col_end)
+                        unit7<R>(Q, stage, col0, c, uib, e & 0xffffu, n, bs.M, bs.B, bs.best);
                     bs.B = warp_min_int(bs.B);
                     if (bs.B < bs.G) {  // publish the warp's best
                         const uint64_t k = warp_min_u64(bs.best);
@@ -711,7 +717,7 @@ static cudaError_t launch_sweep5_g(const SweepLaunch& L, cudaStream_t s, bool pr
                                     attr_bytes(sweep5_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel5<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
-                                                           L.st);
+                                                           L.margin, L.st);
     return cudaGetLastError();
 }
 
@@ -742,7 +748,7 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
                                     attr_bytes(sweep6_smem_bytes(kMaxTileCols)));
     }
     sweep_kernel6<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
-                                                           L.st);
+                                                           L.margin, L.st);
     return cudaGetLastError();
 }
 
@@ -787,7 +793,7 @@ static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool pre
     tile_filter_kernel<<<fgrid, 256, 0, s>>>(L.n, rows_per_tile, L.cb, L.wbox, L.wmax, L.rbox,
                                              L.rmax, L.work, L.workctl, L.st);
     sweep_boxed_kernel<R, NW><<<grid, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.cb, L.wbox, L.wmax,
-                                                          L.work, L.workctl, L.st);
+                                                          L.work, L.margin, L.workctl, L.st);
     return cudaGetLastError();
 }
 

@@ -111,7 +111,23 @@ struct Best5 {
     int B;             // best exact delta known (own or published)
     int G;             // best delta this thread has published or read
     bool busy;         // stage 2 ran in the current window
+    float M;           // bound on |exact - approximate delta| (filter_margin of the instance)
 };
+
+// Last test before the exact distances of a pair that passed the squared
+// screens: the approximate delta (contracted sums of squares, MUFU square
+// roots) against B + M, in the MUFU screen's own form and rounding order
+// (sweep_core.cuh), whose margin M = filter_margin(diag) bounds |exact delta
+// - approximate delta| for every pair.  A pair whose exact delta is <= B
+// always passes; the squared screens test each distance against V = B +
+// e[i] + e[c] on its own, this one their sum, which is what removes most
+// exact evaluations where long edges make V large.
+__device__ __forceinline__ bool approx_delta_pass(float xr, float yr, float xq, float yq,
+                                                  const OrderedCity& q, const OrderedCity& qp,
+                                                  int ei, int B, float M) {
+    const float v = approx_dist(xr, yr, q.x, q.y) + (approx_dist(xq, yq, qp.x, qp.y) - q.e);
+    return v < (float)(B + ei) + M;
+}
 
 // Stage 3 for the rows whose bit is set in `rows`: per-pair squared test with
 // the exact e[c], then the exact delta.  q = column c, qp = column c - 1.
@@ -128,10 +144,11 @@ __device__ __forceinline__ void column_exact5(RowBlock5<R>& rb, uint32_t rows,
         const float xq = row_x5<R>(rb, r - 1), yq = row_y5<R>(rb, r - 1);
         const float u = rb.T2[r] + q.e;
         const float L = u * fabsf(u);
-        if (fmaxf(sq_dist(xr, yr, q.x, q.y), sq_dist(xq, yq, qp.x, qp.y)) < L) {
+        const int ei = (int)rb.T2[r] - bs.B - 5;  // rows that reach here have pairs
+        if (fmaxf(sq_dist(xr, yr, q.x, q.y), sq_dist(xq, yq, qp.x, qp.y)) < L &&
+            approx_delta_pass(xr, yr, xq, yq, q, qp, ei, bs.B, bs.M)) {
             const int d1 = exact_dist(xr, yr, q.x, q.y);
             const int d2 = exact_dist(xq, yq, qp.x, qp.y);
-            const int ei = (int)rb.T2[r] - bs.B - 5;  // rows that reach here have pairs
             const int delta = d1 + d2 - ei - ec;
             if (delta <= bs.B) {
                 const uint64_t key = pack_key(delta, i, c);

@@ -161,10 +161,11 @@ __device__ __forceinline__ void column_rest6(RowBlock6<R>& rb, uint32_t rows, co
         const float xq = rb.gx[r], yq = rb.gy[r];
         const float u = rb.T2[r] + q.e;
         const float L = u * fabsf(u);
-        if (fmaxf(sq_dist(xr, yr, q.x, q.y), sq_dist(xq, yq, qp.x, qp.y)) < L) {
+        const int ei = (int)rb.T2[r] - bs.B - 5;  // rows that reach here have pairs
+        if (fmaxf(sq_dist(xr, yr, q.x, q.y), sq_dist(xq, yq, qp.x, qp.y)) < L &&
+            approx_delta_pass(xr, yr, xq, yq, q, qp, ei, bs.B, bs.M)) {
             const int d1 = exact_dist(xr, yr, q.x, q.y);
             const int d2 = exact_dist(xq, yq, qp.x, qp.y);
-            const int ei = (int)rb.T2[r] - bs.B - 5;  // rows that reach here have pairs
             const int delta = d1 + d2 - ei - ec;
             if (delta <= bs.B) {
                 const uint64_t key = pack_key(delta, i, c);

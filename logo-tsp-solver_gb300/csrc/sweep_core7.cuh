@@ -27,6 +27,7 @@
 #pragma once
 #include <cfloat>
 #include "sweep_core3.cuh"
+#include "sweep_core5.cuh"
 
 namespace logo {
 
@@ -86,31 +87,53 @@ __device__ __forceinline__ uint32_t rows_open7(const RowBlock7<R>& rb, float4 w,
 }
 
 // One unit: rows uib + r (bit r of rm) against column c (this lane's
-// column of the window; c < col_end).  stg[k] = column col0 - 1 + k.
+// column of the window; c < col_end).  stg[k] = column col0 - 1 + k.  The
+// unit's rows are read from global memory (L2) all at once for R <= 8, so a
+// unit waits for one round trip rather than one per open row (heavy tiles
+// queue tens of units per warp).
+template <int R>
+__device__ __forceinline__ void unit_pair7(const OrderedCity& a, const OrderedCity& ap,
+                                           const OrderedCity& q, const OrderedCity& qp,
+                                           uint32_t i, uint32_t c, float M, int& B,
+                                           uint64_t& best) {
+    const int ei = (int)a.e, ec = (int)q.e;
+    const float u = (float)(B + ei + 5) + q.e;
+    const float L = u * fabsf(u);
+    if (fmaxf(sq_dist(a.x, a.y, q.x, q.y), sq_dist(ap.x, ap.y, qp.x, qp.y)) < L &&
+        approx_delta_pass(a.x, a.y, ap.x, ap.y, q, qp, ei, B, M)) {
+        const int d1 = exact_dist(a.x, a.y, q.x, q.y);
+        const int d2 = exact_dist(ap.x, ap.y, qp.x, qp.y);
+        const int delta = d1 + d2 - ei - ec;
+        if (delta <= B) {
+            const uint64_t key = pack_key(delta, i, c);
+            best = key < best ? key : best;
+            B = delta < B ? delta : B;
+        }
+    }
+}
+
 template <int R>
 __device__ __forceinline__ void unit7(const OrderedCity* Q, const OrderedCity* stg,
                                       uint32_t col0, uint32_t c, uint32_t uib, uint32_t rm,
-                                      uint32_t n, int& B, uint64_t& best) {
+                                      uint32_t n, float M, int& B, uint64_t& best) {
     const uint32_t k = c - col0 + 1;
     const OrderedCity q = stg[k], qp = stg[k - 1];
-    const int ec = (int)q.e;
+    if constexpr (R <= 8) {
+        OrderedCity rw[R + 1];  // rows uib - 1 .. uib + R - 1 (uib >= 1)
+#pragma unroll
+        for (int t = 0; t <= R; ++t) rw[t] = Q[min(uib - 1 + t, n - 1)];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t i = uib + r;
+            if (!((rm >> r) & 1u) || c < i + 2 || i + 3 > n) continue;
+            unit_pair7<R>(rw[r + 1], rw[r], q, qp, i, c, M, B, best);
+        }
+    } else {
 #pragma unroll 1
-    for (uint32_t m = rm; m; m &= m - 1) {
-        const uint32_t i = uib + (__ffs(m) - 1);
-        if (c < i + 2 || i + 3 > n) continue;
-        const OrderedCity a = Q[i], ap = Q[i - 1];
-        const int ei = (int)a.e;
-        const float u = (float)(B + ei + 5) + q.e;
-        const float L = u * fabsf(u);
-        if (fmaxf(sq_dist(a.x, a.y, q.x, q.y), sq_dist(ap.x, ap.y, qp.x, qp.y)) < L) {
-            const int d1 = exact_dist(a.x, a.y, q.x, q.y);
-            const int d2 = exact_dist(ap.x, ap.y, qp.x, qp.y);
-            const int delta = d1 + d2 - ei - ec;
-            if (delta <= B) {
-                const uint64_t key = pack_key(delta, i, c);
-                best = key < best ? key : best;
-                B = delta < B ? delta : B;
-            }
+        for (uint32_t m = rm; m; m &= m - 1) {
+            const uint32_t i = uib + (__ffs(m) - 1);
+            if (c < i + 2 || i + 3 > n) continue;
+            unit_pair7<R>(Q[i], Q[i - 1], q, qp, i, c, M, B, best);
         }
     }
 }

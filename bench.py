@@ -207,9 +207,9 @@ SWEEP_KERNELS = {0: ("sweep_kernel", "MUFU screen"),
                  6: ("sweep_boxed_kernel", "boxed screen: near-neighbour seed bound, row-block "
                                            "and window bounding boxes, then the local-coordinate "
                                            "screen")}
-# kernels per sweep launch: the boxed variant runs window_stats_kernel, seed_kernel and
-# tile_filter_kernel first
-SWEEP_LAUNCHES = {6: 4}
+# kernels per sweep launch: the boxed variant runs window_seed_kernel and tile_filter_kernel
+# first
+SWEEP_LAUNCHES = {6: 3}
 
 
 def profile_figures(name):
@@ -349,7 +349,7 @@ def run_ours(a, world, rank, local, dist):
            "call": "logo_descend(max_moves=1) per step: route H2D, sweep, argmin, "
                    "reversal, route D2H"}
 
-    # roofline of the sweep (the dominant kernel: the boxed screen's four
+    # roofline of the sweep (the dominant kernel: the boxed screen's three
     # launches, timed together by the events around logo_enqueue_sweep)
     info = s.info()
     kname, screen = SWEEP_KERNELS[info["variant"]]
@@ -360,7 +360,7 @@ def run_ours(a, world, rank, local, dist):
     roof = {"bound": "alu", "unit": "TOPS (lane operations)"}
     roof.update(lane_roofline(pairs, mean_sweep_s, sm_max, profile_figures(prof_name)))
     roof.update({
-        "kernel": ("logo::window_stats_kernel + logo::seed_kernel + logo::tile_filter_kernel + "
+        "kernel": ("logo::window_seed_kernel + logo::tile_filter_kernel + "
                    if SWEEP_LAUNCHES.get(info["variant"]) else "")
                   + f"logo::{kname}<{info['rows_per_thread']},{info['warps_per_cta']}>"
                   + f" ({screen}, {info['tile_cols']}-column tiles; timed together)",

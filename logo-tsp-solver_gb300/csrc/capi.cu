@@ -98,6 +98,7 @@ TourBufs bufs(const logo_ctx* c) {
     T.n = c->n;
     T.st = c->d_st;
     T.seen = c->d_seen;
+    T.pos = c->d_pos;
     return T;
 }
 
@@ -150,8 +151,11 @@ void default_shape(uint32_t n, int& R, int& NW, uint32_t& cb, int& variant) {
         variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 512;
     } else if (n >= 50000) {
+        // with the seeded bound, 64-column tiles (n = 100k descent from the NN
+        // tour: 1.37 s against 1.47 s with 128, 1.41 with 32; sweep of the
+        // benchmark's states 0.074 ms against 0.080)
         variant = LOGO_SWEEP_BOXED;
-        R = 4; NW = 4; cb = 128;
+        R = 4; NW = 4; cb = 64;
     } else if (n >= 17500) {
         variant = LOGO_SWEEP_BOXED;
         R = 4; NW = 4; cb = 64;
@@ -216,6 +220,9 @@ logo_status rebuild(logo_ctx* c) {
         std::vector<uint32_t> nb((size_t)c->n * kSeedNeighbours);
         knn_grid(h.data(), c->n, kSeedNeighbours, nb.data());
         CK(c, cudaMalloc(&c->d_pos, sizeof(uint32_t) * c->n));
+        // positions are written by every kernel that moves the tour; until a
+        // route is uploaded they only need to be in range
+        CK(c, cudaMemset(c->d_pos, 0, sizeof(uint32_t) * c->n));
         CK(c, cudaMalloc(&c->d_nbr, sizeof(uint32_t) * nb.size()));
         CK(c, cudaMemcpy(c->d_nbr, nb.data(), sizeof(uint32_t) * nb.size(),
                          cudaMemcpyHostToDevice));
@@ -686,7 +693,7 @@ logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_
     CKC(cudaMalloc(&c->d_wmax, sizeof(float) * sweep_windows(n)));
     CKC(cudaMalloc(&c->d_rbox, sizeof(float4) * sweep_row_windows(n)));
     CKC(cudaMalloc(&c->d_rmax, sizeof(float) * sweep_row_windows(n)));
-    CKC(cudaMalloc(&c->d_workctl, 2 * sizeof(uint32_t)));
+    CKC(cudaMalloc(&c->d_workctl, 3 * sizeof(uint32_t)));
     c->coop_grid = coop_grid(n, device);
     c->coop_ils_grid = c->coop_grid > 0 ? coop_ils_grid(n, device) : 0;
     if (c->coop_grid > 0) CKC(cudaMalloc(&c->d_coop, sizeof(CoopSync)));

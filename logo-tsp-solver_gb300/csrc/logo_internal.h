@@ -25,13 +25,13 @@ struct SweepLaunch {
     // bounding box and largest edge (sweep_windows(n) entries), the same per
     // 32-row window (rows 1 + 32g .., sweep_row_windows(n) entries), the list
     // of (tile, column-window mask) that pass the window test (ntiles entries)
-    // and its two counters (items, items claimed)
+    // and its three counters (tiles listed from the start, claimed, listed from the end)
     float4* wbox;
     float* wmax;
     float4* rbox;
     float* rmax;
-    uint4* work;
-    uint32_t* workctl;
+    uint4* work;         // ntiles entries
+    uint32_t* workctl;   // tiles listed from the start, claimed, listed from the end
     // boxed variant: the tour's city ids (both buffers), the tour position of
     // every city (written by the window pass) and kSeedNeighbours nearest
     // neighbours per city, whose pairs seed the sweep's best delta
@@ -72,6 +72,9 @@ struct TourBufs {
     uint32_t n;
     DevState* st;
     uint32_t* seen;  // (n + 31) / 32 words, zero before launch_init_ordered
+    // tour position of every city (boxed sweep's seed pass; null otherwise),
+    // kept current by every kernel that moves the tour
+    uint32_t* pos;
 };
 // Cooperative persistent descent (coop.cu) for tours up to kCoopMaxN cities:
 // one launch runs the descent to a local optimum or st->max_moves.

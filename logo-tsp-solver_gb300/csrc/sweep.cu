@@ -265,8 +265,9 @@ __global__ void __launch_bounds__(NW * 32)
 // .. 3 + 32 g + 31, below n) the bounding box of its coordinates and its
 // largest edge, and the same for every window of 32 rows (rows 1 + 32 g ..,
 // only rows with pairs, i + 3 <= n; a window without such rows gets an
-// empty box and -3e7), one warp per window.  Also clears the work-list
-// counters of pass 2.
+// empty box and -3e7), one warp per window, together with the seed of the
+// sweep's bound (seed_position for the warp's 32 positions).  Also clears
+// the work-list counters of pass 2.
 __device__ __forceinline__ void window_reduce(float& m, float& x0, float& x1, float& y0,
                                               float& y1) {
     for (int o = 16; o; o >>= 1) {
@@ -278,23 +279,76 @@ __device__ __forceinline__ void window_reduce(float& m, float& x0, float& x1, fl
     }
 }
 
-__global__ void __launch_bounds__(256)
-    window_stats_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                        const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
-                        uint32_t* __restrict__ pos, uint32_t n, float4* __restrict__ wbox,
-                        float* __restrict__ wmax, float4* __restrict__ rbox,
-                        float* __restrict__ rmax, uint32_t* __restrict__ workctl, DevState* st) {
-    if (*(volatile unsigned int*)&st->converged) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        workctl[0] = 0u;
-        workctl[1] = 0u;
+// Seed of the sweep's bound at tour position i: for each of the
+// kSeedNeighbours nearest neighbours v of its city (at position p = pos[v]),
+// the two pairs whose move creates the short edge (i, p): (a, b) =
+// (min, max) of (i, p), whose delta has d(a, b) = d(i, p) as its first term,
+// and (a + 1, b + 1), which has it as its second.  Their exact deltas are
+// real pairs of this sweep, so the best of them is a valid starting bound:
+// the sweep's best delta is at most that, and the tile filter and the boxed
+// kernel prune with it from the start instead of with -1.  The lowest key
+// goes to st->best_key, where it competes with every other pair, so the
+// chosen move is still the exact lowest (delta, i, c).  Any p the position
+// array gives names a real pair, so a stale entry costs seed quality only.
+__device__ __forceinline__ void seed_position(const OrderedCity* __restrict__ Q,
+                                              const uint32_t* __restrict__ R,
+                                              const uint32_t* __restrict__ pos,
+                                              const uint32_t* __restrict__ nbr, uint32_t n,
+                                              uint32_t i, uint64_t& best) {
+    constexpr uint32_t K = kSeedNeighbours;
+    // every load of the position's candidates is issued before any is used
+    const uint32_t t = min(R[i], n - 1);
+    const OrderedCity qi = Q[i], qim = Q[i >= 1 ? i - 1 : 0], qip = Q[min(i + 1, n - 1)];
+    uint32_t p[K];
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) p[k] = nbr[(size_t)t * K + k];
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) p[k] = min(pos[min(p[k], n - 1)], n - 1);
+    OrderedCity qp[K], qpm[K], qpp[K];
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) {
+        qp[k] = Q[p[k]];
+        qpm[k] = Q[p[k] >= 1 ? p[k] - 1 : 0];
+        qpp[k] = Q[min(p[k] + 1, n - 1)];
     }
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) {
+        const uint32_t a = min(i, p[k]), b = max(i, p[k]);
+        if (b < a + 2) continue;  // also p == i
+        const int D = exact_dist(qi.x, qi.y, qp[k].x, qp[k].y);
+        const int ee = (int)qi.e + (int)qp[k].e;
+        if (a >= 1) {
+            // pair (a, b): d(a, b) + d(a - 1, b - 1) - e[a] - e[b]
+            const int delta = D + exact_dist(qim.x, qim.y, qpm[k].x, qpm[k].y) - ee;
+            if (delta < 0) {
+                const uint64_t key = pack_key(delta, a, b);
+                best = key < best ? key : best;
+            }
+        }
+        if (b + 1 <= n - 1) {
+            // pair (a + 1, b + 1): d(a + 1, b + 1) + d(a, b) - e[a + 1] - e[b + 1]
+            const int delta = exact_dist(qip.x, qip.y, qpp[k].x, qpp[k].y) + D -
+                              (int)qip.e - (int)qpp[k].e;
+            if (delta < 0) {
+                const uint64_t key = pack_key(delta, a + 1, b + 1);
+                best = key < best ? key : best;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    window_seed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
+                       const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
+                       const uint32_t* __restrict__ pos, const uint32_t* __restrict__ nbr,
+                       uint32_t n, float4* __restrict__ wbox, float* __restrict__ wmax,
+                       float4* __restrict__ rbox, float* __restrict__ rmax,
+                       uint32_t* __restrict__ workctl, DevState* st) {
+    if (*(volatile unsigned int*)&st->converged) return;
+    if (blockIdx.x == 0 && threadIdx.x < 3) workctl[threadIdx.x] = 0u;
     const bool cur = *(volatile unsigned int*)&st->cur;
     const OrderedCity* Q = cur ? Q1 : Q0;
-    // tour position of every city, for the seed pass
     const uint32_t* R = cur ? R1 : R0;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        pos[min(R[k], n - 1)] = k;
     const uint32_t g = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (g < sweep_windows(n)) {  // whole warps
         const uint32_t c = 3 + g * kWin6 + lane;
@@ -322,73 +376,13 @@ __global__ void __launch_bounds__(256)
             rmax[g] = m;
         }
     }
-}
-
-// Boxed variant, seed pass: for every tour position i and each of the
-// kSeedNeighbours nearest neighbours v of its city (at position p = pos[v]),
-// the two pairs whose move creates the short edge (i, p): (a, b) =
-// (min, max) of (i, p), whose delta has d(a, b) = d(i, p) as its first term,
-// and (a + 1, b + 1), which has it as its second.  Their exact deltas are
-// real pairs of this sweep, so the best of them is a valid starting bound:
-// the sweep's best delta is at most that, and the tile filter and the boxed
-// kernel prune with it from the start instead of with -1.  The lowest key
-// goes to st->best_key, where it competes with every other pair, so the
-// chosen move is still the exact lowest (delta, i, c).
-__global__ void __launch_bounds__(256)
-    seed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
-                const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
-                const uint32_t* __restrict__ pos, const uint32_t* __restrict__ nbr, uint32_t n,
-                DevState* st) {
-    constexpr uint32_t K = kSeedNeighbours;
-    if (*(volatile unsigned int*)&st->converged) return;
-    const bool cur = *(volatile unsigned int*)&st->cur;
-    const OrderedCity* Q = cur ? Q1 : Q0;
-    const uint32_t* R = cur ? R1 : R0;
+    // the seed: positions 3 + 32 g + lane, and 0, 1, 2 in the first warp
     uint64_t best = kNoMove;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        // every load of a position's candidates is issued before any is used
-        const uint32_t t = min(R[i], n - 1);
-        const OrderedCity qi = Q[i], qim = Q[i >= 1 ? i - 1 : 0], qip = Q[min(i + 1, n - 1)];
-        uint32_t p[K];
-#pragma unroll
-        for (uint32_t k = 0; k < K; ++k) p[k] = nbr[(size_t)t * K + k];
-#pragma unroll
-        for (uint32_t k = 0; k < K; ++k) p[k] = min(pos[min(p[k], n - 1)], n - 1);
-        OrderedCity qp[K], qpm[K], qpp[K];
-#pragma unroll
-        for (uint32_t k = 0; k < K; ++k) {
-            qp[k] = Q[p[k]];
-            qpm[k] = Q[p[k] >= 1 ? p[k] - 1 : 0];
-            qpp[k] = Q[min(p[k] + 1, n - 1)];
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < K; ++k) {
-            const uint32_t a = min(i, p[k]), b = max(i, p[k]);
-            if (b < a + 2) continue;  // also p == i
-            const int D = exact_dist(qi.x, qi.y, qp[k].x, qp[k].y);
-            const int ee = (int)qi.e + (int)qp[k].e;
-            if (a >= 1) {
-                // pair (a, b): d(a, b) + d(a - 1, b - 1) - e[a] - e[b]
-                const int delta = D + exact_dist(qim.x, qim.y, qpm[k].x, qpm[k].y) - ee;
-                if (delta < 0) {
-                    const uint64_t key = pack_key(delta, a, b);
-                    best = key < best ? key : best;
-                }
-            }
-            if (b + 1 <= n - 1) {
-                // pair (a + 1, b + 1): d(a + 1, b + 1) + d(a, b) - e[a + 1] - e[b + 1]
-                const int delta = exact_dist(qip.x, qip.y, qpp[k].x, qpp[k].y) + D -
-                                  (int)qip.e - (int)qpp[k].e;
-                if (delta < 0) {
-                    const uint64_t key = pack_key(delta, a + 1, b + 1);
-                    best = key < best ? key : best;
-                }
-            }
-        }
-    }
+    const uint32_t i = 3 + g * kWin6 + lane;
+    if (i < n) seed_position(Q, R, pos, nbr, n, i, best);
+    if (g == 0 && lane < 3 && lane < n) seed_position(Q, R, pos, nbr, n, lane, best);
     best = warp_min_u64(best);
-    if ((threadIdx.x & 31) == 0 && best != kNoMove)
-        atomicMin(&st->best_key, (unsigned long long)best);
+    if (lane == 0 && best != kNoMove) atomicMin(&st->best_key, (unsigned long long)best);
 }
 
 // Boxed variant, pass 2: gridDim.y CTAs per row block (the rows of one tile
@@ -403,11 +397,32 @@ __global__ void __launch_bounds__(256)
 // (row0, col0, mask of their column windows that passed).  The tiles are
 // the ones the tile list holds: columns from row0 + 2 to n - 1 in steps of
 // cb.
+// Steps (32 column windows each) per filter warp on the longest row block:
+// fewer, longer-lived CTAs share the per-CTA start (the bound, the row
+// block's windows and their union) over several steps (measured on GB300:
+// n = 100k sweep of the benchmark's states 0.0645 ms with 4, 0.0688 with 1,
+// 0.0655 with 8; n = 1M random tour 0.208 ms with 8, 0.232 with 4).
+__host__ __device__ constexpr uint32_t filter_steps(uint32_t n) { return n >= 300000 ? 8u : 4u; }
+
+// Tiles the filter lists first: those whose rows and columns are close
+// along the tour (the tile meets its row block's own positions), which on
+// tours built or improved by local moves are close in space too, so most of
+// their rows stay open and they are the longest items; starting them first
+// keeps them off the end of the sweep.  Every other tile is listed from the
+// end of the array.
+__device__ __forceinline__ bool front_tile(uint32_t row0, uint32_t col0, uint32_t rows_per_tile,
+                                           uint32_t mask, uint32_t wpt) {
+    (void)mask;
+    (void)wpt;
+    return col0 < row0 + 2 + rows_per_tile;
+}
+
 __global__ void __launch_bounds__(256)
     tile_filter_kernel(uint32_t n, uint32_t rows_per_tile, uint32_t cb,
                        const float4* __restrict__ wbox, const float* __restrict__ wmax,
                        const float4* __restrict__ rbox, const float* __restrict__ rmax,
-                       uint4* __restrict__ work, uint32_t* __restrict__ workctl, DevState* st) {
+                       uint4* __restrict__ work, uint32_t cap, uint32_t* __restrict__ workctl,
+                       DevState* st) {
     __shared__ float4 srb[kMaxTileRows / kWin6];
     __shared__ float sre[kMaxTileRows / kWin6];
     if (*(volatile unsigned int*)&st->converged) return;
@@ -475,9 +490,13 @@ __global__ void __launch_bounds__(256)
         if (lane < tps && t0 + lane < ntiles) {
             const uint32_t mask =
                 (votes >> (lane * wpt)) & (wpt == 32 ? 0xffffffffu : ((1u << wpt) - 1u));
-            if (mask)
-                work[atomicAdd(&workctl[0], 1u)] =
-                    make_uint4(row0, col_start + (t0 + lane) * cb, mask, 0u);
+            if (mask) {
+                const uint32_t col0 = col_start + (t0 + lane) * cb;
+                const uint32_t k = front_tile(row0, col0, rows_per_tile, mask, wpt)
+                                       ? atomicAdd(&workctl[0], 1u)
+                                       : cap - 1u - atomicAdd(&workctl[2], 1u);
+                work[k] = make_uint4(row0, col0, mask, 0u);
+            }
         }
     }
 }
@@ -544,7 +563,8 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
     sweep_boxed_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                        uint32_t n, uint32_t cb, const float4* __restrict__ gbox,
                        const float* __restrict__ gmax, const uint4* __restrict__ work,
-                       float margin, uint32_t* __restrict__ workctl, DevState* st) {
+                       uint32_t cap, float margin, uint32_t* __restrict__ workctl,
+                       DevState* st) {
     static_assert(R <= 16 && NW * 32 <= 256, "unit encoding: 8-bit thread, 16-bit rows");
     constexpr int G = (128 / R) < 32 ? (128 / R) : 32;
     extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -560,7 +580,9 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
 
     if (*(volatile unsigned int*)&st->converged) return;
     const OrderedCity* Q = (*(volatile unsigned int*)&st->cur) ? Q1 : Q0;
-    const uint32_t items = workctl[0];
+    // the filter's list: items [0, front) from the start, the rest from the end
+    const uint32_t front = workctl[0];
+    const uint32_t items = front + workctl[2];
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
@@ -585,7 +607,7 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
             slot->walk = 0u;
             slot->rows = 0u;
             slot->best = *(volatile unsigned long long*)&st->best_key;
-            if (idx < items) slot->item = work[idx];
+            if (idx < items) slot->item = work[idx < front ? idx : cap - 1u - (idx - front)];
         }
         __syncthreads();  // the slot is ready (the previous tile ended in a barrier)
         if (slot->idx >= items) break;
@@ -752,8 +774,8 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
     return cudaGetLastError();
 }
 
-// Boxed variant: window statistics (and city positions), near-neighbour
-// seed, tile filter, persistent sweep (one CTA per resident slot).
+// Boxed variant: window statistics with the near-neighbour seed, tile
+// filter, persistent sweep (one CTA per resident slot).
 template <int R, int NW>
 static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool prepare) {
     const size_t smem = boxed_smem_bytes(L.cb, NW);
@@ -781,19 +803,20 @@ static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool pre
     }
     const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
     const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
-    window_stats_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.n, L.wbox,
-                                                       L.wmax, L.rbox, L.rmax, L.workctl, L.st);
-    const uint32_t sgrid = (L.n + 255) / 256 < 4096 ? (L.n + 255) / 256 : 4096;
-    seed_kernel<<<sgrid, 256, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.nbr, L.n, L.st);
+    window_seed_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.nbr, L.n,
+                                                      L.wbox, L.wmax, L.rbox, L.rmax,
+                                                      L.workctl, L.st);
     const uint32_t rows_per_tile = (uint32_t)(NW * 32 * R);
     const uint32_t row_blocks = (L.n - 4) / rows_per_tile + 1;  // row0 + 3 <= n
-    // CTAs per row block: one step per warp for the longest row (block 0)
+    // CTAs per row block: filter_steps(n) steps per warp for the longest row (block 0)
     const uint32_t steps = ((L.n - 3 + L.cb - 1) / L.cb + 32 / (L.cb / 32) - 1) / (32 / (L.cb / 32));
-    const dim3 fgrid(row_blocks, (steps + 7) / 8);
+    const uint32_t fs = filter_steps(L.n);
+    const dim3 fgrid(row_blocks, (steps + 8 * fs - 1) / (8 * fs));
     tile_filter_kernel<<<fgrid, 256, 0, s>>>(L.n, rows_per_tile, L.cb, L.wbox, L.wmax, L.rbox,
-                                             L.rmax, L.work, L.workctl, L.st);
+                                             L.rmax, L.work, L.ntiles, L.workctl, L.st);
     sweep_boxed_kernel<R, NW><<<grid, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.cb, L.wbox, L.wmax,
-                                                          L.work, L.margin, L.workctl, L.st);
+                                                          L.work, L.ntiles, L.margin, L.workctl,
+                                                          L.st);
     return cudaGetLastError();
 }
 

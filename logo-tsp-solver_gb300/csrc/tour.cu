@@ -4,7 +4,11 @@
 // The tour lives in two buffers (Q[cur], route[cur]); every permutation is a
 // gather from buffer cur into buffer cur^1 followed by a flip of cur made by
 // the last CTA to finish (threadfence + counter, no spinning), so the host
-// never touches the tour between moves.
+// never touches the tour between moves.  Where the context keeps city
+// positions (the boxed sweep's seed pass), every kernel that moves the tour
+// writes them too; a position left stale (the cooperative descent does not
+// write them) only weakens the seed, never a result, because the seed pass
+// evaluates whatever pair of positions it reads exactly.
 //   init_ordered_kernel    ≙ ordered-coordinate gather, CUDASolver.cpp:316-319
 //   apply_move_kernel      ≙ rotate + reverse, twoOptLocalSolver.cpp:41-48
 //   tour_length_kernel     ≙ routeLength, headers.h:170-189
@@ -47,7 +51,8 @@ __device__ __forceinline__ bool last_block_done(unsigned int* counter) {
 __global__ void init_ordered_kernel(const float2* __restrict__ xy,
                                     const uint32_t* __restrict__ route,
                                     OrderedCity* __restrict__ Q, uint32_t n,
-                                    uint32_t* __restrict__ seen, DevState* st) {
+                                    uint32_t* __restrict__ seen, uint32_t* __restrict__ pos,
+                                    DevState* st) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x) {
         uint32_t v = route[k], w = route[k == 0 ? n - 1 : k - 1];
@@ -55,6 +60,7 @@ __global__ void init_ordered_kernel(const float2* __restrict__ xy,
         bool bad = v >= n;
         if (!bad) bad = atomicOr(&seen[v >> 5], 1u << (v & 31)) & (1u << (v & 31));
         if (bad) st->bad_route = 1u;
+        else if (pos) pos[v] = k;
         v = v < n ? v : 0u;
         w = w < n ? w : 0u;
         const float2 a = xy[v];
@@ -85,7 +91,7 @@ __device__ __forceinline__ void gather_tour(const OrderedCity* __restrict__ Qs,
                                             const uint32_t* __restrict__ Rs,
                                             OrderedCity* __restrict__ Qd,
                                             uint32_t* __restrict__ Rd, uint32_t n,
-                                            Src src) {
+                                            uint32_t* __restrict__ pos, Src src) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x) {
         const uint32_t s = src(k);
@@ -98,7 +104,9 @@ __device__ __forceinline__ void gather_tour(const OrderedCity* __restrict__ Qs,
         o.e = (float)exact_dist(b.x, b.y, a.x, a.y);
         o.pad = 0.f;
         Qd[k] = o;
-        Rd[k] = Rs[s];
+        const uint32_t id = Rs[s];
+        Rd[k] = id;
+        if (pos) pos[min(id, n - 1)] = k;
     }
 }
 
@@ -124,7 +132,8 @@ __global__ void apply_move_kernel(TourBufs T) {
         }
         return;
     }
-    gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1], cur ? T.route[0] : T.route[1], n,
+    gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1],
+                cur ? T.route[0] : T.route[1], n, T.pos,
                 [=] __device__(uint32_t k) { return rotrev_src(k, p, q, n); });
     if (last_block_done(&st->done_blocks)) {
         const unsigned long long m = st->moves;
@@ -183,13 +192,15 @@ __global__ void kick_kernel(TourBufs T, int kind) {
         if (c[2] < c[1]) { t = c[1]; c[1] = c[2]; c[2] = t; }
         if (c[1] < c[0]) { t = c[0]; c[0] = c[1]; c[1] = t; }
         const uint32_t p1 = c[0], p2 = c[1], p3 = c[2];
-        gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1], cur ? T.route[0] : T.route[1], n,
+        gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1],
+                    cur ? T.route[0] : T.route[1], n, T.pos,
                     [=] __device__(uint32_t k) { return bridge_src(k, p1, p2, p3); });
     } else {
         uint32_t a = uniform_below(rng, n);
         uint32_t b = uniform_below(rng, n);
         if (b < a) { uint32_t t = a; a = b; b = t; }
-        gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1], cur ? T.route[0] : T.route[1], n,
+        gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1],
+                    cur ? T.route[0] : T.route[1], n, T.pos,
                     [=] __device__(uint32_t k) { return rotrev_src(k, a, b, n); });
     }
     if (last_block_done(&st->done_blocks)) {
@@ -219,7 +230,9 @@ __global__ void accept_kernel(TourBufs T) {
             T.route_best[k] = Rc[k];
         } else {
             Qc[k] = T.Qbest[k];
-            Rc[k] = T.route_best[k];
+            const uint32_t id = T.route_best[k];
+            Rc[k] = id;
+            if (T.pos) T.pos[min(id, T.n - 1)] = k;
         }
     }
     if (last_block_done(&st->done_blocks)) {
@@ -312,7 +325,7 @@ cudaError_t launch_route_check_reset(const TourBufs& T, cudaStream_t s) {
 
 cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s) {
     init_ordered_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, T.route[0], T.Q[0], T.n,
-                                                           T.seen, T.st);
+                                                           T.seen, T.pos, T.st);
     return cudaGetLastError();
 }
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,

@@ -582,10 +582,16 @@ void destroy(logo_ctx* c) {
     delete c;
 }
 
+// Device time of a call (CUDA events on the context's stream); a timer made
+// with on = false records nothing and stop() returns 0 without waiting.
 struct Timer {
     logo_ctx* c;
-    explicit Timer(logo_ctx* cc) : c(cc) { cudaEventRecord(c->ev0, c->stream); }
+    bool on;
+    explicit Timer(logo_ctx* cc, bool enabled = true) : c(cc), on(enabled) {
+        if (on) cudaEventRecord(c->ev0, c->stream);
+    }
     double stop() {
+        if (!on) return 0.0;
         cudaEventRecord(c->ev1, c->stream);
         ++c->host_waits;
         cudaEventSynchronize(c->ev1);
@@ -930,7 +936,7 @@ static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves
     if (!c) return LOGO_ERR_INVALID_ARG;
     if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
-    Timer t(c);
+    Timer t(c, stats != nullptr);  // no stats: no timing and no extra wait
     logo_status s = upload_route(c, route);
     if (s != LOGO_OK) return s;
     uint64_t start_len = 0, final_len = 0, moves = 0, sweeps = 0;

@@ -145,7 +145,8 @@ def cmd_construct(a):
     [50, 2000], uniform fp32 in [0,1e4)^2): nearest-neighbour tours built on
     the host (logo_nn_tour, one instance after another) and then solved, vs
     built by the batched launch itself (start=START_NN); both then descend to
-    a local optimum.  Also the multiple-fragment tours' host time."""
+    a local optimum.  The same for multiple-fragment tours (logo_mf_tour on
+    the host vs start=START_MF, built by a launch before the solve)."""
     coords, _, seeds = instances.batched_workload(a.count, a.seed, 50, 2000, 1.0e4)
     total = sum(len(c) for c in coords)
     t0 = time.perf_counter()
@@ -162,7 +163,14 @@ def cmd_construct(a):
         t0 = time.perf_counter()
         r_dev, res_dev, ms_dev = b.solve(coords, None, seeds, start=lg.START_NN)
         dev_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r_mfg, _, ms_mfg = b.solve(coords, mf, seeds)
+        mf_given_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r_mfd, _, ms_mfd = b.solve(coords, None, seeds, start=lg.START_MF)
+        mf_dev_s = time.perf_counter() - t0
     same = all(np.array_equal(x, y) for x, y in zip(r_given, r_dev))
+    same_mf = all(np.array_equal(x, y) for x, y in zip(r_mfg, r_mfd))
     print(json.dumps({"workload": f"construct: {a.count} instances, n log-uniform [50,2000], "
                                   "NN start tours, descent to a local optimum",
                       "host_nn_s": host_nn_s, "host_mf_s": host_mf_s,
@@ -170,7 +178,11 @@ def cmd_construct(a):
                       "solve_device_nn_device_ms": ms_dev, "solve_device_nn_wall_s": dev_s,
                       "device_construction_ms": ms_dev - ms_given,
                       "end_to_end_host_nn_s": host_nn_s + given_s,
-                      "end_to_end_device_nn_s": dev_s, "identical_results": same}))
+                      "end_to_end_device_nn_s": dev_s, "identical_results": same,
+                      "solve_given_mf_device_ms": ms_mfg, "solve_device_mf_device_ms": ms_mfd,
+                      "device_mf_construction_ms": ms_mfd - ms_mfg,
+                      "end_to_end_host_mf_s": host_mf_s + mf_given_s,
+                      "end_to_end_device_mf_s": mf_dev_s, "identical_results_mf": same_mf}))
 
 
 def _pool(count, seed, n_lo, n_hi):

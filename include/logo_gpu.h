@@ -216,11 +216,15 @@ typedef struct logo_batch_shape {
     int tile_cols;
 } logo_batch_shape;
 
-/* Start tours of a batch: the routes passed in, or nearest-neighbour tours
- * built on the device (equal to logo_nn_tour from city 0; the routes are then
- * outputs only). */
+/* Start tours of a batch: the routes passed in, or tours built on the device
+ * (the routes are then outputs only): nearest-neighbour tours equal to
+ * logo_nn_tour from city 0, built by each instance's solving CTA, or
+ * multiple-fragment tours equal to logo_mf_tour, built by one CTA per
+ * instance in a launch before the solve (initRoute_KD_NN and
+ * multipleFragment_KD, src/utils/kdtree_utils.c:279-301 and 56-242). */
 #define LOGO_START_GIVEN 0
 #define LOGO_START_NN 1
+#define LOGO_START_MF 2
 
 typedef struct logo_batch_opts {
     int device;

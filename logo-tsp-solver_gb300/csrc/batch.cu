@@ -194,6 +194,330 @@ __device__ void nn_tour_cta(const float2* xy, uint32_t n, uint32_t* route, uint3
     }
 }
 
+// ---- multiple-fragment start tour, built by the CTA --------------------------
+// The same steps as the host logo_mf_tour (csrc/construct.cpp), itself the
+// steps of multipleFragment_KD (src/utils/kdtree_utils.c:56-242): every city
+// links to its nearest other city; a priority queue of (nint distance to the
+// link, city) is popped shortest first; a city of degree 2 is dropped, a
+// link that is no longer usable (degree 2, or the far end of the city's own
+// fragment) is looked up again among the cities of degree < 2 and the city
+// re-queued; otherwise the two fragments are joined.  The host queue is
+// std::priority_queue ordered by distance alone, so cities of equal distance
+// leave it in the order of its sift steps; one thread replays those steps
+// exactly (the standard binary heap: push sifts the new element up from the
+// end; pop moves the hole from the root down to a leaf along the child that
+// comes first, then sifts the former last element up from there), and the
+// CTA answers the nearest-city queries as nn_tour_cta does (binary32 screen,
+// double decision, lowest id on ties).  State in shared memory: the heap
+// (8n bytes), 16-bit links and fragment ends, 8-bit degrees (together 13n
+// bytes), 16-bit neighbours in join order (4n bytes); n <= 4096.  A kernel
+// of its own (mf_start_kernel) builds every instance's tour before the
+// batched solve, which then loads them as given tours.
+struct MfFrag {
+    int d;
+    uint32_t id;
+};
+
+// a comes after b in the host's queue (its top is the shortest distance)
+__device__ __forceinline__ bool mf_after(const MfFrag& a, const MfFrag& b) { return a.d > b.d; }
+
+__device__ void mf_sift_up(MfFrag* H, int hole, int top, MfFrag v) {
+    int parent = (hole - 1) / 2;
+    while (hole > top && mf_after(H[parent], v)) {
+        H[hole] = H[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    H[hole] = v;
+}
+
+__device__ void mf_push(MfFrag* H, int& len, MfFrag v) {
+    mf_sift_up(H, len, 0, v);
+    ++len;
+}
+
+__device__ void mf_pop(MfFrag* H, int& len) {
+    const int nl = len - 1;
+    const MfFrag v = H[nl];
+    int hole = 0, child = 0;
+    while (child < (nl - 1) / 2) {
+        child = 2 * (child + 1);
+        if (mf_after(H[child], H[child - 1])) --child;
+        H[hole] = H[child];
+        hole = child;
+    }
+    if ((nl & 1) == 0 && child == (nl - 2) / 2) {
+        child = 2 * (child + 1);
+        H[hole] = H[child - 1];
+        hole = child - 1;
+    }
+    mf_sift_up(H, hole, 0, v);
+    len = nl;
+}
+
+__device__ __forceinline__ double mf_ddist(float2 a, float2 b) {
+    const double ex = __dsub_rn((double)a.x, (double)b.x);
+    const double ey = __dsub_rn((double)a.y, (double)b.y);
+    return __dsqrt_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)));
+}
+
+// One thread's nearest other city to city i among all cities (the initial
+// links): binary32 squared distances screen, double decides, lowest id wins.
+__device__ uint32_t mf_nearest_all(const float2* xy, uint32_t n, uint32_t i) {
+    const float2 p = xy[i];
+    float m = INFINITY;
+    for (uint32_t j = 0; j < n; ++j) {
+        if (j == i) continue;
+        const float2 q = xy[j];
+        const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y);
+        m = fminf(m, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    }
+    const float thr = m * (1.0f + 1e-6f) + 1e-30f;
+    double bd = INFINITY;
+    uint32_t bi = i;
+    for (uint32_t j = 0; j < n; ++j) {
+        if (j == i) continue;
+        const float2 q = xy[j];
+        const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y);
+        if (__fmaf_rn(dy, dy, __fmul_rn(dx, dx)) > thr) continue;
+        const double d = mf_ddist(p, q);
+        if (d < bd) {  // j ascending: equal distances keep the lower id
+            bd = d;
+            bi = j;
+        }
+    }
+    return bi;
+}
+
+// The CTA's nearest city to city x among those of degree < 2, other than x
+// and skip; n (none) if there is no such city.  Every thread returns it.
+template <int NT>
+__device__ uint32_t mf_nearest_cta(const float2* xy, uint32_t n, uint32_t x, uint32_t skip,
+                                   const uint8_t* degree) {
+    __shared__ float red_f[NT / 32];
+    __shared__ double red_d[NT / 32];
+    __shared__ uint32_t red_i[NT / 32];
+    __shared__ uint32_t pick;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float2 p = xy[x];
+    float m = INFINITY;
+    for (uint32_t j = threadIdx.x; j < n; j += NT) {
+        if (j == x || j == skip || degree[j] >= 2) continue;
+        const float2 q = xy[j];
+        const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y);
+        m = fminf(m, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    }
+    for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) red_f[warp] = m;
+    __syncthreads();
+    m = red_f[0];
+#pragma unroll
+    for (int w = 1; w < NT / 32; ++w) m = fminf(m, red_f[w]);
+    const float thr = m * (1.0f + 1e-6f) + 1e-30f;
+    double bd = INFINITY;
+    uint32_t bi = 0xFFFFFFFFu;
+    for (uint32_t j = threadIdx.x; j < n; j += NT) {
+        if (j == x || j == skip || degree[j] >= 2) continue;
+        const float2 q = xy[j];
+        const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y);
+        if (__fmaf_rn(dy, dy, __fmul_rn(dx, dx)) > thr) continue;
+        const double d = mf_ddist(p, q);
+        if (d < bd || (d == bd && j < bi)) {
+            bd = d;
+            bi = j;
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (od < bd || (od == bd && oi < bi)) {
+            bd = od;
+            bi = oi;
+        }
+    }
+    if (lane == 0) {
+        red_d[warp] = bd;
+        red_i[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double d = red_d[0];
+        uint32_t i = red_i[0];
+        for (int w = 1; w < NT / 32; ++w)
+            if (red_d[w] < d || (red_d[w] == d && red_i[w] < i)) {
+                d = red_d[w];
+                i = red_i[w];
+            }
+        pick = i < n ? i : n;
+    }
+    __syncthreads();
+    const uint32_t r = pick;
+    __syncthreads();
+    return r;
+}
+
+template <int NT>
+__device__ void mf_tour_cta(const float2* xy, uint32_t n, uint32_t* route, unsigned char* qbuf,
+                            uint32_t* bbuf) {
+    __shared__ int ctl;
+    __shared__ uint32_t cx, cy, cskip;
+    __shared__ int hlen;
+    __shared__ bool failed;
+    if (n <= 2) {  // as the host: nothing to join
+        for (uint32_t k = threadIdx.x; k < n; k += NT) route[k] = k;
+        __syncthreads();
+        return;
+    }
+    MfFrag* H = reinterpret_cast<MfFrag*>(qbuf);
+    uint16_t* link = reinterpret_cast<uint16_t*>(qbuf + 8 * (size_t)n);
+    uint16_t* tail = link + n;
+    uint8_t* degree = reinterpret_cast<uint8_t*>(qbuf + 12 * (size_t)n);
+    int16_t* first = reinterpret_cast<int16_t*>(bbuf);
+    int16_t* second = first + n;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        tail[i] = (uint16_t)i;
+        degree[i] = 0;
+        first[i] = -1;
+        second[i] = -1;
+        link[i] = (uint16_t)mf_nearest_all(xy, n, i);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int len = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            const float2 a = xy[i], b = xy[link[i]];
+            mf_push(H, len, MfFrag{exact_dist(a.x, a.y, b.x, b.y), i});
+        }
+        hlen = len;
+        failed = false;
+    }
+    __syncthreads();
+    // Between two joins a city is looked up again at most once (its new link
+    // stays valid until the next join), so n * n bounds the look-ups of a
+    // valid run; the count only guards the loop against a broken state.
+    uint32_t requeries = 0;
+    const uint32_t max_requeries = n * n + 64u;
+    for (uint32_t e = 0; e + 1 < n && !failed; ++e) {
+        for (;;) {
+            if (threadIdx.x == 0) {
+                int len = hlen;
+                while (len > 0 && degree[H[0].id] == 2) mf_pop(H, len);
+                hlen = len;
+                if (len == 0) {
+                    failed = true;
+                    ctl = 0;
+                } else {
+                    const uint32_t x = H[0].id, y = link[x];
+                    cx = x;
+                    if (degree[y] < 2 && y != tail[x]) {
+                        ctl = 0;
+                        cy = y;
+                    } else {
+                        ctl = 1;
+                        cskip = degree[x] ? tail[x] : x;
+                    }
+                }
+            }
+            __syncthreads();
+            if (ctl == 0) break;
+            if (++requeries > max_requeries) {  // the same in every thread
+                if (threadIdx.x == 0) failed = true;
+                __syncthreads();
+                break;
+            }
+            const uint32_t nx = mf_nearest_cta<NT>(xy, n, cx, cskip, degree);
+            if (threadIdx.x == 0) {
+                if (nx >= n) {
+                    failed = true;
+                } else {
+                    const uint32_t x = cx;
+                    link[x] = (uint16_t)nx;
+                    int len = hlen;
+                    mf_pop(H, len);
+                    const float2 a = xy[x], b = xy[nx];
+                    mf_push(H, len, MfFrag{exact_dist(a.x, a.y, b.x, b.y), x});
+                    hlen = len;
+                }
+            }
+            __syncthreads();
+            if (failed) break;
+        }
+        if (failed) break;
+        if (threadIdx.x == 0) {
+            const uint32_t x = cx, y = cy;
+            const uint32_t vs[2] = {x, y};
+            for (int t = 0; t < 2; ++t) {
+                const uint32_t v = vs[t], w = t == 0 ? y : x;
+                if (degree[v] == 0)
+                    first[v] = (int16_t)w;
+                else
+                    second[v] = (int16_t)w;
+                degree[v] = (uint8_t)(degree[v] + 1);
+            }
+            const uint32_t tx = tail[x];
+            tail[tx] = tail[y];
+            tail[tail[y]] = (uint16_t)tx;
+        }
+        __syncthreads();
+    }
+    // list the path from city 0: the part through first[0] reversed, 0, then
+    // the part through second[0]
+    if (threadIdx.x == 0 && !failed) {
+        uint32_t len_before = 0;
+        int from = 0, at = first[0];
+        while (at >= 0 && len_before < n) {
+            ++len_before;
+            const int nx = first[at] == from ? second[at] : first[at];
+            from = at;
+            at = nx;
+        }
+        uint32_t k = len_before, count = 0;
+        from = 0;
+        at = first[0];
+        while (at >= 0 && k > 0) {
+            route[--k] = (uint32_t)at;
+            ++count;
+            const int nx = first[at] == from ? second[at] : first[at];
+            from = at;
+            at = nx;
+        }
+        k = len_before;
+        if (k < n) route[k++] = 0;
+        from = 0;
+        at = second[0];
+        while (at >= 0 && k < n) {
+            route[k++] = (uint32_t)at;
+            const int nx = first[at] == from ? second[at] : first[at];
+            from = at;
+            at = nx;
+        }
+        if (k != n || count != len_before) failed = true;
+    }
+    __syncthreads();
+    if (failed)  // not reached for valid input; the tour stays a permutation
+        for (uint32_t k = threadIdx.x; k < n; k += NT) route[k] = k;
+    __syncthreads();
+}
+
+constexpr int kMfThreads = 256;
+
+__global__ void __launch_bounds__(kMfThreads)
+    mf_start_kernel(const float2* __restrict__ coords, uint32_t* __restrict__ routes,
+                    const BatchInstance* __restrict__ inst, const uint32_t* __restrict__ order,
+                    uint32_t count, uint32_t max_n) {
+    extern __shared__ __align__(16) unsigned char mf_smem[];
+    unsigned char* qbuf = mf_smem;
+    uint32_t* bbuf = reinterpret_cast<uint32_t*>(mf_smem + ((13 * (size_t)max_n + 15) & ~(size_t)15));
+    for (uint32_t k = blockIdx.x; k < count; k += gridDim.x) {
+        const BatchInstance I = inst[order[k]];
+        mf_tour_cta<kMfThreads>(coords + I.off, I.n, routes + I.off, qbuf, bbuf);
+    }
+}
+
+size_t mf_smem_bytes(uint32_t max_n) {
+    return ((13 * (size_t)max_n + 15) & ~(size_t)15) + 4 * (size_t)max_n;
+}
+
 template <int R, int NT, int TC>
 __global__ void __launch_bounds__(NT)
     batch_kernel(BatchArgs A) {
@@ -218,9 +542,9 @@ __global__ void __launch_bounds__(NT)
         uint32_t* rio = A.routes + I.off;
 
         // load (or build) the start tour, its ordered coordinates and edge lengths
-        if (A.start_nn) nn_tour_cta<NT>(xy, n, route, bestr);
+        if (A.start == kStartNN) nn_tour_cta<NT>(xy, n, route, bestr);
         for (uint32_t k = threadIdx.x; k < n; k += NT) {
-            const uint32_t c = A.start_nn ? route[k] : rio[k];
+            const uint32_t c = A.start == kStartNN ? route[k] : rio[k];
             const float2 p = xy[c];
             route[k] = c;
             bestr[k] = c;
@@ -376,6 +700,22 @@ int batch_shapes(BatchShape* out, int cap) {
     LOGO_BATCH_SHAPES(X)
 #undef X
     return k;
+}
+
+cudaError_t prepare_mf_start() {
+    // one limit for every batch: the largest instance's
+    return cudaFuncSetAttribute(mf_start_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)mf_smem_bytes(kBatchMaxN));
+}
+
+cudaError_t launch_mf_start(const float2* coords, uint32_t* routes, const BatchInstance* inst,
+                            const uint32_t* order, uint32_t count, uint32_t max_n, int sms,
+                            cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>(count, (uint32_t)(sms > 0 ? sms : 1) * 4u);
+    mf_start_kernel<<<grid, kMfThreads, mf_smem_bytes(max_n), s>>>(coords, routes, inst, order,
+                                                                  count, max_n);
+    return cudaGetLastError();
 }
 
 }  // namespace logo

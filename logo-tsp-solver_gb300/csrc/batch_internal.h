@@ -6,6 +6,8 @@
 
 namespace logo {
 
+constexpr int kStartGiven = 0, kStartNN = 1, kStartMF = 2;
+
 constexpr uint32_t kBatchMaxN = 4096;  // largest instance a CTA holds in smem
 
 constexpr uint32_t kNoGroup = 0xFFFFFFFFu;
@@ -54,7 +56,7 @@ struct BatchArgs {
     int kick_kind;
     SharedBest* shared;       // per group (null when no instance has a group)
     uint32_t* shared_tours;   // the groups' best tours
-    int start_nn;             // build nearest-neighbour start tours instead of loading them
+    int start;                // kStartGiven, or kStartNN: build nearest-neighbour tours instead of loading them
 };
 
 struct BatchShape {
@@ -66,6 +68,14 @@ struct BatchShape {
 size_t batch_smem_bytes(uint32_t max_n);
 // Launches the persistent kernel with `grid` CTAs; with occupancy != null
 // only reports CTAs per SM for this shape and max_n.
+// Multiple-fragment start tours of instances order[0 .. count) written into
+// routes (equal to logo_mf_tour), one CTA per instance at a time;
+// prepare_mf_start (outside any stream capture) raises the kernel's shared
+// memory limit first.
+cudaError_t prepare_mf_start();
+cudaError_t launch_mf_start(const float2* coords, uint32_t* routes, const BatchInstance* inst,
+                            const uint32_t* order, uint32_t count, uint32_t max_n, int sms,
+                            cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& A, const BatchShape& sh, int grid, cudaStream_t s,
                          int* occupancy);
 // Lists the compiled shapes; returns how many there are.

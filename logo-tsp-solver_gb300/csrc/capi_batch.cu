@@ -211,7 +211,7 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
     if (fixed && !shape_compiled(BatchShape{o.shape.rows_per_thread, o.shape.threads_per_cta,
                                             o.shape.tile_cols}))
         return bfail(b, LOGO_ERR_INVALID_ARG, "shape is not compiled");
-    if (o.start != LOGO_START_GIVEN && o.start != LOGO_START_NN)
+    if (o.start != LOGO_START_GIVEN && o.start != LOGO_START_NN && o.start != LOGO_START_MF)
         return bfail(b, LOGO_ERR_INVALID_ARG, "unknown start-tour kind");
     logo_status s = pack(b, in, count, o.start == LOGO_START_GIVEN);
     if (s != LOGO_OK) return s;
@@ -253,8 +253,15 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
     }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    uint32_t max_n_all = 0;
+    for (uint32_t k = 0; k < count; ++k) max_n_all = std::max(max_n_all, b->h_inst[k].n);
+    if (o.start == LOGO_START_MF) BCK(b, prepare_mf_start());
     BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t ce = cudaSuccess;
+    // multiple-fragment start tours: built first, then loaded as given tours
+    if (o.start == LOGO_START_MF)
+        ce = launch_mf_start(b->d_coords, b->d_routes, b->d_inst, b->d_order, count, max_n_all,
+                             b->sms, b->stream);
     for (size_t gi = 0; gi < groups.size() && ce == cudaSuccess && gi < 8; ++gi) {
         BatchArgs A;
         A.coords = b->d_coords;
@@ -269,7 +276,7 @@ logo_status run(logo_batch* b, const logo_instance* in, uint32_t count,
         A.kick_kind = o.kick_kind;
         A.shared = share ? b->d_shared : nullptr;
         A.shared_tours = share ? b->d_shared_tours : nullptr;
-        A.start_nn = o.start == LOGO_START_NN;
+        A.start = o.start == LOGO_START_NN ? kStartNN : kStartGiven;
         ce = launch_batch(A, groups[gi].shape, grids[gi], b->stream, nullptr);
     }
     cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);

@@ -30,6 +30,7 @@ DESCENT_GRAPH = 1
 DESCENT_COOPERATIVE = 2
 START_GIVEN = 0
 START_NN = 1
+START_MF = 2
 MAX_CITIES = 2097152
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "DEVICE_FAULT",
@@ -512,7 +513,7 @@ class Batch:
     def solve(self, coords_list, routes, seeds, kicks=0, kind=KICK_SEGMENT, shape=None, ctas=0,
               start=START_GIVEN):
         """Returns (routes, results as a list of dicts, device_ms).  With
-        start=START_NN the routes are built on the device (routes may be None)."""
+        start=START_NN or START_MF the routes are built on the device (routes may be None)."""
         if routes is None:
             routes = [np.zeros(len(np.asarray(c).reshape(-1, 2)), np.uint32) for c in coords_list]
         arr, xs, rs = self._pack(coords_list, routes, seeds)

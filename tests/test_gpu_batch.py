@@ -178,3 +178,39 @@ def test_batch_nn_start_built_on_device(lg, inst, kicks):
                 assert r["best_length"] == st["final_length"]
             assert r["start_length"] == st["start_length"]
         assert np.array_equal(g, want), len(xy)
+
+
+@pytest.mark.parametrize("kicks", [0, 4])
+def test_batch_mf_start_built_on_device(lg, inst, kicks):
+    """start=START_MF: a launch before the solve builds each instance's
+    multiple-fragment tour (the host queue's order of equal distances
+    replayed); start lengths and results equal the single-instance path
+    started from the host logo_mf_tour.  Covered: 3-5 cities, integer grids
+    with many equal distances and duplicate points, uniform and clustered
+    instances up to the batch maximum of 4,096 cities."""
+    coords, seeds = [], []
+    for k, n in enumerate([3, 4, 5, 60, 97, 300, 1000, 2000, 3000, 4096]):
+        s = 900 + k
+        if k % 3 == 0:
+            xy = inst.uniform_int(n, s)
+            xy = np.floor(xy / 50.0).astype(np.float32)  # many ties and duplicates
+        elif k % 3 == 1:
+            xy = inst.uniform_f32(n, s, 1.0e4)
+        else:
+            xy = inst.clustered(n, s, side=1.0e6, clusters=max(2, n // 200))
+        coords.append(xy)
+        seeds.append(s)
+    total = sum(len(c) for c in coords)
+    with lg.Batch(len(coords), total) as b:
+        got, res, _ = b.solve(coords, None, seeds, kicks=kicks, start=lg.START_MF)
+    for xy, g, r, s in zip(coords, got, res, seeds):
+        mf = lg.mf_tour(xy)
+        assert r["status"] == 0
+        with lg.Solver(xy) as sol:
+            assert r["start_length"] == sol.route_length(mf), len(xy)
+            if kicks:
+                want, st = sol.ils(mf, kicks, s, lg.KICK_SEGMENT)
+            else:
+                want, st = sol.optimize(mf)
+            assert r["best_length"] == st["final_length"]
+        assert np.array_equal(g, want), len(xy)

@@ -442,6 +442,8 @@ typedef struct logo_ctx_info {
     int cooperative_ctas; /* CTAs of the cooperative descent; 0 if unavailable */
     uint64_t host_waits;  /* times this context's calls have waited on the device so far
                              (one logo_ils call: a fixed handful, whatever the kick count) */
+    int route_io;         /* LOGO_ROUTE_IO_COPY or LOGO_ROUTE_IO_DIRECT in use */
+    int pad0;
 } logo_ctx_info;
 
 logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
@@ -464,6 +466,23 @@ logo_status logo_ctx_set_shape(logo_ctx *ctx, int rows_per_thread, int warps_per
 #define LOGO_DESCENT_COOPERATIVE 2
 /* INVALID_ARG for an unknown mode, or COOPERATIVE where it is unavailable. */
 logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
+
+/* How the route buffers of logo_descend, logo_ils, logo_best_move,
+ * logo_tour_length, logo_set_route and logo_get_route reach the device; both
+ * give identical results.
+ * LOGO_ROUTE_IO_AUTO (default): DIRECT where the device can read and write
+ *   pageable host memory (cudaDevAttrPageableMemoryAccess, e.g. a coherent
+ *   CPU-GPU link), else COPY.
+ * LOGO_ROUTE_IO_COPY: cudaMemcpyAsync from and to the caller's buffer.
+ * LOGO_ROUTE_IO_DIRECT: the load and store kernels read and write the
+ *   caller's buffer in place (one wait per logo_descend call instead of two).
+ * Route buffers must then be valid for n uint32_t, as for a copy. */
+#define LOGO_ROUTE_IO_AUTO 0
+#define LOGO_ROUTE_IO_COPY 1
+#define LOGO_ROUTE_IO_DIRECT 2
+/* INVALID_ARG for an unknown mode, or DIRECT where the device cannot reach
+ * pageable host memory. */
+logo_status logo_ctx_set_route_io(logo_ctx *ctx, int mode);
 
 /* Sweep kernel variants; all return identical moves (the default depends on
  * n, see logo_ctx_info.variant).

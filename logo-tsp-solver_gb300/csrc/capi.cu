@@ -33,7 +33,10 @@ struct logo_ctx {
     uint32_t* d_route_best = nullptr;
     DevState* d_st = nullptr;
     DevState* h_st = nullptr;  // pinned mirror
-    uint32_t* d_seen = nullptr;   // bitmap of the route permutation check
+    uint32_t* d_seen = nullptr;   // route permutation check: last load that met each city
+    uint32_t load_epoch = 0;      // loads so far (mod 2^32 - 1, from 1)
+    int route_io = LOGO_ROUTE_IO_AUTO;
+    bool pageable_ok = false;     // the device reads and writes pageable host memory
     float4* d_wbox = nullptr;     // per-window boxes and largest edges (boxed sweep)
     float* d_wmax = nullptr;
     float4* d_rbox = nullptr;
@@ -383,20 +386,38 @@ logo_status build_ils_graph(logo_ctx* c) {
     return LOGO_OK;
 }
 
-// Uploads a route and builds the ordered tour.  Whether the route is a
-// permutation of 0..n-1 is checked on the device by the gather (a host
-// check cost about 80 us per call at n = 100k, a tenth of a sweep);
-// read_state reports a bad route as LOGO_ERR_INVALID_ARG, and a descent on
-// it converges before any sweep.
-// The route is copied straight from and to the caller's buffer: measured on
-// GB300 (n = 100k, 400 KB) 11 us each way, against 19 us (in) and 23 us
-// (out) through a pinned staging buffer and a host memcpy.
-logo_status upload_route(logo_ctx* c, const uint32_t* route) {
+// Route transfer: the device reads and writes the caller's buffer in place
+// when it can reach pageable host memory (cudaDevAttrPageableMemoryAccess,
+// e.g. over a coherent CPU-GPU link; LOGO_ROUTE_IO_AUTO), else the buffer
+// is copied with cudaMemcpyAsync (LOGO_ROUTE_IO_COPY).
+bool route_direct(const logo_ctx* c) {
+    return c->route_io == LOGO_ROUTE_IO_DIRECT ||
+           (c->route_io == LOGO_ROUTE_IO_AUTO && c->pageable_ok);
+}
+
+// Uploads a route and builds the ordered tour in one launch.  Whether the
+// route is a permutation of 0..n-1 is checked on the device by the same
+// launch (a host check cost about 80 us per call at n = 100k, a tenth of a
+// sweep); read_state reports a bad route as LOGO_ERR_INVALID_ARG, and a
+// descent on it converges before any sweep.  With reset_moves != 0 the
+// launch also prepares a descent of at most reset_moves moves.
+// Copy mode copies straight from the caller's buffer: measured on GB300
+// (n = 100k, 400 KB) 11 us each way, against 19 us (in) and 23 us (out)
+// through a pinned staging buffer and a host memcpy.
+logo_status upload_route(logo_ctx* c, const uint32_t* route,
+                         unsigned long long reset_moves = 0) {
     if (!route) return fail(c, LOGO_ERR_INVALID_ARG, "route is NULL");
-    CK(c, cudaMemcpyAsync(c->d_route[0], route, sizeof(uint32_t) * c->n,
-                          cudaMemcpyHostToDevice, c->stream));
-    CK(c, launch_route_check_reset(bufs(c), c->stream));
-    CK(c, launch_init_ordered(bufs(c), c->stream));
+    const uint32_t* src = route;
+    if (!route_direct(c)) {
+        CK(c, cudaMemcpyAsync(c->d_route[0], route, sizeof(uint32_t) * c->n,
+                              cudaMemcpyHostToDevice, c->stream));
+        src = c->d_route[0];
+    }
+    if (++c->load_epoch == 0xFFFFFFFFu) {  // every value seen holds is stale again
+        CK(c, cudaMemsetAsync(c->d_seen, 0, sizeof(uint32_t) * c->n, c->stream));
+        c->load_epoch = 1;
+    }
+    CK(c, launch_load_route(bufs(c), src, c->load_epoch, reset_moves, c->stream));
     c->have_route = true;
     return LOGO_OK;
 }
@@ -440,7 +461,9 @@ logo_status status_to_error(logo_ctx* c, unsigned int st) {
 
 // Descent on the resident tour.  Replays the chunk graph until the device
 // reports convergence (or the move limit).
-logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0);
+logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0,
+                          uint32_t* route_out, bool* route_stored);
+logo_status enqueue_route_out(logo_ctx* c, uint32_t* route, bool best);
 
 // Cooperative descents of this library never overlap on one device: each
 // grid is sized to be resident on its own, and two whose CTAs were only
@@ -455,12 +478,18 @@ bool use_coop(const logo_ctx* c) {
     return c->coop_grid > 0 && c->descent_mode != LOGO_DESCENT_GRAPH;
 }
 
+// reset_enqueued: the reset was folded into the route load just before.
+// route_out (direct route mode only): the caller's buffer, written on the
+// device before the final state read when the descent is known to end there
+// (one wait instead of two); *route_stored says whether it was.
 logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
-                        uint64_t* sweeps_out, bool reset = true) {
+                        uint64_t* sweeps_out, bool reset = true, bool reset_enqueued = false,
+                        uint32_t* route_out = nullptr, bool* route_stored = nullptr) {
     if (max_moves == 0) max_moves = ~0ull >> 1;
-    if (reset)  // also clears the status word
+    if (route_stored) *route_stored = false;
+    if (reset && !reset_enqueued)  // also clears the status word
         CK(c, launch_reset_descent(bufs(c), max_moves, c->stream));
-    else
+    else if (!reset)
         CK(c, cudaMemsetAsync(&c->d_st->status, 0, sizeof(unsigned int), c->stream));
     // a fresh descent starts from zero moves and records its sweep count on
     // the device; a continued one needs the counters first
@@ -488,13 +517,18 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
         {
             std::lock_guard<std::mutex> lk(coop_lock(c->device));
             CK(c, launch_coop_descent(A, c->coop_grid, c->stream));
+            if (route_out) {  // the launch runs the whole descent
+                s = enqueue_route_out(c, route_out, false);
+                if (s != LOGO_OK) return s;
+                if (route_stored) *route_stored = true;
+            }
             s = read_state(c);
         }
         if (s != LOGO_OK) return s;
         if (!c->h_st->converged && !c->h_st->status)
             return fail(c, LOGO_ERR_DEVICE_FAULT, "cooperative descent did not finish");
     } else {
-        logo_status s = graph_descent(c, max_moves, reset, moves0);
+        logo_status s = graph_descent(c, max_moves, reset, moves0, route_out, route_stored);
         if (s != LOGO_OK) return s;
     }
     if (moves_out) *moves_out = c->h_st->moves - moves0;
@@ -507,24 +541,35 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
 
 // Replays the chunk graph (or single steps when fewer moves are allowed than
 // a chunk holds) until the device flags convergence.
-logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0) {
+logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0,
+                          uint32_t* route_out, bool* route_stored) {
     uint64_t before = moves0;
     for (;;) {
         const uint64_t left = max_moves - (before - moves0);
+        bool stored = false;
         if (reset && left < c->chunk_steps) {
-            // fewer moves allowed than a chunk holds: launch just those steps
+            // fewer moves allowed than a chunk holds: launch just those steps,
+            // after which the descent has converged or met its move limit
             const SweepLaunch L = sweep_args(c);
             const TourBufs T = bufs(c);
             for (uint64_t k = 0; k < left; ++k) {
                 CK(c, launch_sweep(L, c->stream));
                 CK(c, launch_apply_move(T, c->stream));
             }
+            if (route_out) {
+                logo_status s = enqueue_route_out(c, route_out, false);
+                if (s != LOGO_OK) return s;
+                stored = true;
+            }
         } else {
             CK(c, cudaGraphLaunch(c->chunk_exec, c->stream));
         }
         logo_status s = read_state(c);
         if (s != LOGO_OK) return s;
-        if (c->h_st->converged || c->h_st->status) break;
+        if (c->h_st->converged || c->h_st->status) {
+            if (route_stored) *route_stored = stored;
+            break;
+        }
         // every replay applies at least one move or converges
         if (c->h_st->moves == before)
             return fail(c, LOGO_ERR_DEVICE_FAULT, "descent made no progress");
@@ -533,10 +578,23 @@ logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t 
     return LOGO_OK;
 }
 
-logo_status download_route(logo_ctx* c, uint32_t* route, bool best) {
+// Enqueues the transfer of the current (or best) tour into the caller's
+// buffer; download_route also waits for it.  Copy mode reads the current
+// buffer index from the last read_state.
+logo_status enqueue_route_out(logo_ctx* c, uint32_t* route, bool best) {
+    if (route_direct(c)) {
+        CK(c, launch_store_route(bufs(c), route, best, c->stream));
+        return LOGO_OK;
+    }
     const uint32_t* src = best ? c->d_route_best : c->d_route[c->h_st->cur & 1];
     CK(c, cudaMemcpyAsync(route, src, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToHost,
                           c->stream));
+    return LOGO_OK;
+}
+
+logo_status download_route(logo_ctx* c, uint32_t* route, bool best) {
+    logo_status s = enqueue_route_out(c, route, best);
+    if (s != LOGO_OK) return s;
     ++c->host_waits;
     CK(c, cudaStreamSynchronize(c->stream));
     return LOGO_OK;
@@ -694,7 +752,15 @@ logo_status logo_ctx_create(int device, const logo_xy* coords, uint32_t n, logo_
     CKC(cudaMalloc(&c->d_route_best, sizeof(uint32_t) * n));
     CKC(cudaMalloc(&c->d_st, sizeof(DevState)));
     CKC(cudaMallocHost(&c->h_st, sizeof(DevState)));
-    CKC(cudaMalloc(&c->d_seen, sizeof(uint32_t) * ((n + 31) / 32)));
+    CKC(cudaMalloc(&c->d_seen, sizeof(uint32_t) * n));
+    CKC(cudaMemset(c->d_seen, 0, sizeof(uint32_t) * n));
+    {
+        int pageable = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) !=
+            cudaSuccess)
+            pageable = 0;
+        c->pageable_ok = pageable != 0;
+    }
     CKC(cudaMalloc(&c->d_wbox, sizeof(float4) * sweep_windows(n)));
     CKC(cudaMalloc(&c->d_wmax, sizeof(float) * sweep_windows(n)));
     CKC(cudaMalloc(&c->d_rbox, sizeof(float4) * sweep_row_windows(n)));
@@ -734,6 +800,22 @@ logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
     info->descent_mode = use_coop(c) ? LOGO_DESCENT_COOPERATIVE : LOGO_DESCENT_GRAPH;
     info->cooperative_ctas = c->coop_grid;
     info->host_waits = c->host_waits;
+    info->route_io = route_direct(c) ? LOGO_ROUTE_IO_DIRECT : LOGO_ROUTE_IO_COPY;
+    info->pad0 = 0;
+    return LOGO_OK;
+}
+
+logo_status logo_ctx_set_route_io(logo_ctx* c, int mode) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
+    if (mode != LOGO_ROUTE_IO_AUTO && mode != LOGO_ROUTE_IO_COPY &&
+        mode != LOGO_ROUTE_IO_DIRECT)
+        return fail(c, LOGO_ERR_INVALID_ARG, "unknown route transfer mode");
+    if (mode == LOGO_ROUTE_IO_DIRECT && !c->pageable_ok)
+        return fail(c, LOGO_ERR_INVALID_ARG,
+                    "direct route transfer unavailable: the device cannot access pageable "
+                    "host memory");
+    c->route_io = mode;
     return LOGO_OK;
 }
 
@@ -861,13 +943,15 @@ logo_status logo_get_route(logo_ctx* c, uint32_t* route) {
     return download_route(c, route, false);
 }
 
+static logo_status sweep_once(logo_ctx* c, logo_move* out, bool reset_enqueued);
+
 logo_status logo_best_move(logo_ctx* c, const uint32_t* route, logo_move* out) {
     if (!c || !out) return LOGO_ERR_INVALID_ARG;
     if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
-    logo_status s = upload_route(c, route);
+    logo_status s = upload_route(c, route, ~0ull >> 1);
     if (s != LOGO_OK) return s;
-    return logo_sweep_resident(c, out);
+    return sweep_once(c, out, true);
 }
 
 logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
@@ -875,7 +959,12 @@ logo_status logo_sweep_resident(logo_ctx* c, logo_move* out) {
     if (c->poisoned) return poisoned_error(c);
     if (!c->have_route) return fail(c, LOGO_ERR_INVALID_ARG, "no resident route");
     CK(c, cudaSetDevice(c->device));
-    CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));  // clears status too
+    return sweep_once(c, out, false);
+}
+
+static logo_status sweep_once(logo_ctx* c, logo_move* out, bool reset_enqueued) {
+    if (!reset_enqueued)
+        CK(c, launch_reset_descent(bufs(c), ~0ull >> 1, c->stream));  // clears status too
     CK(c, launch_sweep(sweep_args(c), c->stream));
     logo_status s = read_state(c);
     if (s != LOGO_OK) return s;
@@ -937,7 +1026,11 @@ static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves
     if (c->poisoned) return poisoned_error(c);
     CK(c, cudaSetDevice(c->device));
     Timer t(c, stats != nullptr);  // no stats: no timing and no extra wait
-    logo_status s = upload_route(c, route);
+    // without stats or a trace nothing runs between the load and the descent:
+    // the load also resets the descent, and in direct route mode the result
+    // is written back before the one final wait
+    const bool quick = !stats && !(trace && trace_cap);
+    logo_status s = upload_route(c, route, quick ? (max_moves ? max_moves : ~0ull >> 1) : 0);
     if (s != LOGO_OK) return s;
     uint64_t start_len = 0, final_len = 0, moves = 0, sweeps = 0;
     if (stats) {
@@ -954,7 +1047,9 @@ static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves
         CK(c, cudaMemcpyAsync(&c->d_st->log_cap, &cap32, sizeof(cap32),
                               cudaMemcpyHostToDevice, c->stream));
     }
-    s = run_descent(c, max_moves, &moves, &sweeps);
+    bool stored = false;
+    s = run_descent(c, max_moves, &moves, &sweeps, true, quick,
+                    quick && route_direct(c) ? route : nullptr, &stored);
     if (d_log) {
         int* null_log = nullptr;
         const unsigned int zero = 0;
@@ -975,7 +1070,7 @@ static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves
         s = length_now(c, &final_len);
         if (s != LOGO_OK) return s;
     }
-    s = download_route(c, route, false);
+    if (!stored) s = download_route(c, route, false);
     const double ms = t.stop();
     if (s != LOGO_OK) return s;
     if (stats) {

@@ -58,7 +58,7 @@ struct DevState {
     unsigned int done_blocks;       // last-block-done counter
     unsigned int log_cap;
     unsigned int len_done;          // last-block counter of the length sum
-    unsigned int bad_route;         // set by the gather: the route is not a permutation
+    unsigned int bad_route;         // the last loaded route is not a permutation
     int* move_log;                  // (delta, i, j) per move, or null
     unsigned long long length_acc;  // partial sums of tour_length_kernel
     // ILS run on the device (one graph or one cooperative launch per call)
@@ -67,7 +67,7 @@ struct DevState {
     unsigned long long ils_iters;   // kick-loop passes so far (guard)
     unsigned long long start_length; // length of the tour the call started from
     unsigned int kick_kind;         // LOGO_KICK_SEGMENT or LOGO_KICK_DOUBLE_BRIDGE
-    unsigned int ils_pad;
+    unsigned int load_bad;          // set by a CTA of load_route_kernel that met a bad id
 };
 
 __host__ __device__ __forceinline__ uint64_t pack_key(int delta, uint32_t i,

@@ -71,7 +71,7 @@ struct TourBufs {
     const float2* xy;
     uint32_t n;
     DevState* st;
-    uint32_t* seen;  // (n + 31) / 32 words, zero before launch_init_ordered
+    uint32_t* seen;  // n words: number of the last route load that met each city
     // tour position of every city (boxed sweep's seed pass; null otherwise),
     // kept current by every kernel that moves the tour
     uint32_t* pos;
@@ -113,12 +113,17 @@ cudaError_t launch_coop_ils(const CoopArgs& A, int grid, cudaStream_t s);
 // One CTA waits at the cooperative grid barrier sized for two (test hook).
 cudaError_t launch_barrier_probe(CoopSync* cs, DevState* st, cudaStream_t s);
 
-// Builds Q[0] from xy and route[0] (route already uploaded to route[0]) and
-// checks that route[0] is a permutation of 0..n-1 (st->bad_route = 1 if not;
-// out-of-range entries are read as city 0).
-// Clears the seen bitmap, bad_route and cur; call before launch_init_ordered.
-cudaError_t launch_route_check_reset(const TourBufs& T, cudaStream_t s);
-cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s);
+// Loads a tour from src (a host buffer the device reads in place, or a
+// device copy) into route[0] and Q[0], with pos and the permutation check
+// (st->bad_route = 1 if src is not a permutation of 0..n-1; `epoch` must
+// differ from every value seen holds, i.e. count loads from 1 with seen
+// zeroed at the start and on wrap-around); cur = 0.  With reset_moves != 0
+// also what launch_reset_descent(reset_moves) does.
+cudaError_t launch_load_route(const TourBufs& T, const uint32_t* src, uint32_t epoch,
+                              unsigned long long reset_moves, cudaStream_t s);
+// Writes the current tour (best: the ILS best) to dst (host buffer written
+// in place, or device memory).
+cudaError_t launch_store_route(const TourBufs& T, uint32_t* dst, bool best, cudaStream_t s);
 // Prepares *st for a new descent: cur = 0 kept, counters cleared.
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,
                                  cudaStream_t s);

@@ -48,30 +48,66 @@ __device__ __forceinline__ bool last_block_done(unsigned int* counter) {
     return false;
 }
 
-__global__ void init_ordered_kernel(const float2* __restrict__ xy,
-                                    const uint32_t* __restrict__ route,
-                                    OrderedCity* __restrict__ Q, uint32_t n,
-                                    uint32_t* __restrict__ seen, uint32_t* __restrict__ pos,
-                                    DevState* st) {
+// Loads a tour from src (the caller's buffer read in place, or a device
+// copy of it): route[0] = src (when src is not route[0] itself), Q[0] =
+// the ordered cities with their incoming edges, pos = the position of every
+// city, and the permutation check: seen[v] holds the number of the last
+// load that met city v, so a city met twice in this load (or an id >= n)
+// makes the route bad without clearing anything between loads.  The last
+// CTA to finish sets st->bad_route and st->cur = 0 and, with
+// reset_moves != 0, prepares a descent (the fields reset_descent_kernel
+// sets; nothing to descend on a bad route).  Out-of-range ids are read as
+// city 0 for the coordinates.
+__global__ void load_route_kernel(const float2* __restrict__ xy, const uint32_t* src,
+                                  uint32_t* R0, OrderedCity* __restrict__ Q, uint32_t n,
+                                  uint32_t* __restrict__ seen, uint32_t epoch,
+                                  uint32_t* __restrict__ pos, DevState* st,
+                                  unsigned long long reset_moves) {
+    bool bad = false;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x) {
-        uint32_t v = route[k], w = route[k == 0 ? n - 1 : k - 1];
-        // permutation check: each city marks its bit once
-        bool bad = v >= n;
-        if (!bad) bad = atomicOr(&seen[v >> 5], 1u << (v & 31)) & (1u << (v & 31));
-        if (bad) st->bad_route = 1u;
-        else if (pos) pos[v] = k;
-        v = v < n ? v : 0u;
-        w = w < n ? w : 0u;
+        const uint32_t raw = src[k], rawp = src[k == 0 ? n - 1 : k - 1];
+        bool b = raw >= n;
+        if (!b) b = atomicExch(&seen[raw], epoch) == epoch;
+        bad |= b;
+        if (!b && pos) pos[raw] = k;
+        if (R0 != src) R0[k] = raw;
+        const uint32_t v = raw < n ? raw : 0u, w = rawp < n ? rawp : 0u;
         const float2 a = xy[v];
-        const float2 b = xy[w];
+        const float2 c = xy[w];
         OrderedCity o;
         o.x = a.x;
         o.y = a.y;
-        o.e = (float)exact_dist(b.x, b.y, a.x, a.y);
+        o.e = (float)exact_dist(c.x, c.y, a.x, a.y);
         o.pad = 0.f;
         Q[k] = o;
     }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->load_bad, 1u);
+    if (last_block_done(&st->done_blocks)) {
+        const unsigned int b = atomicExch(&st->load_bad, 0u);
+        st->bad_route = b;
+        st->cur = 0u;
+        if (reset_moves) {
+            st->best_key = kNoMove;
+            st->moves = 0;
+            st->status = 0u;
+            st->converged = b ? 1u : 0u;
+            st->sweeps_at_reset = st->sweeps;
+            st->max_moves = reset_moves;
+        }
+    }
+}
+
+// Writes the current tour (or the best one) to dst, the caller's buffer
+// written in place.
+__global__ void store_route_kernel(const uint32_t* __restrict__ R0,
+                                   const uint32_t* __restrict__ R1,
+                                   const uint32_t* __restrict__ Rbest, uint32_t* dst,
+                                   uint32_t n, const DevState* st, int best) {
+    const uint32_t* R = best ? Rbest : (*(volatile const unsigned int*)&st->cur ? R1 : R0);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += gridDim.x * blockDim.x)
+        dst[k] = R[k];
 }
 
 __global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves) {
@@ -303,31 +339,21 @@ cudaError_t launch_kick_cond(DevState* st, cudaGraphConditionalHandle h, bool fi
     return cudaGetLastError();
 }
 
-// Clears the permutation check before launch_init_ordered: the seen bitmap,
-// the bad-route flag and the current-buffer index (one launch instead of
-// three memsets per uploaded route).
-__global__ void route_check_reset_kernel(uint32_t* __restrict__ seen, uint32_t words,
-                                         DevState* st) {
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < words;
-         k += gridDim.x * blockDim.x)
-        seen[k] = 0u;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->bad_route = 0u;
-        st->cur = 0u;
-    }
-}
-
-cudaError_t launch_route_check_reset(const TourBufs& T, cudaStream_t s) {
-    const uint32_t words = (T.n + 31) / 32;
-    route_check_reset_kernel<<<grid_for(words), kThreads, 0, s>>>(T.seen, words, T.st);
+cudaError_t launch_load_route(const TourBufs& T, const uint32_t* src, uint32_t epoch,
+                              unsigned long long reset_moves, cudaStream_t s) {
+    load_route_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, src, T.route[0], T.Q[0], T.n,
+                                                         T.seen, epoch, T.pos, T.st,
+                                                         reset_moves);
     return cudaGetLastError();
 }
 
-cudaError_t launch_init_ordered(const TourBufs& T, cudaStream_t s) {
-    init_ordered_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, T.route[0], T.Q[0], T.n,
-                                                           T.seen, T.pos, T.st);
+cudaError_t launch_store_route(const TourBufs& T, uint32_t* dst, bool best, cudaStream_t s) {
+    store_route_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.route[0], T.route[1],
+                                                          T.route_best, dst, T.n, T.st,
+                                                          best ? 1 : 0);
     return cudaGetLastError();
 }
+
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,
                                  cudaStream_t s) {
     reset_descent_kernel<<<1, 1, 0, s>>>(T.st, max_moves);

@@ -28,6 +28,9 @@ SWEEP_BOXED = 6
 DESCENT_AUTO = 0
 DESCENT_GRAPH = 1
 DESCENT_COOPERATIVE = 2
+ROUTE_IO_AUTO = 0
+ROUTE_IO_COPY = 1
+ROUTE_IO_DIRECT = 2
 START_GIVEN = 0
 START_NN = 1
 START_MF = 2
@@ -51,7 +54,7 @@ EXPORTS = [
     "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
     "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
     "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
-    "logo_diag_flag_timeout",
+    "logo_diag_flag_timeout", "logo_ctx_set_route_io",
 ]
 
 
@@ -83,7 +86,8 @@ class CtxInfo(ctypes.Structure):
                 ("tile_cols", ctypes.c_uint32), ("tiles", ctypes.c_uint32),
                 ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32),
                 ("variant", ctypes.c_int), ("descent_mode", ctypes.c_int),
-                ("cooperative_ctas", ctypes.c_int), ("host_waits", ctypes.c_uint64)]
+                ("cooperative_ctas", ctypes.c_int), ("host_waits", ctypes.c_uint64),
+                ("route_io", ctypes.c_int), ("pad0", ctypes.c_int)]
 
 
 class Instance(ctypes.Structure):
@@ -174,6 +178,7 @@ def load(path=LIB_PATH):
     L.logo_ctx_set_shape.argtypes = [_vp, c.c_int, c.c_int, c.c_uint32]
     L.logo_ctx_set_kernel.argtypes = [_vp, c.c_int, c.c_int, c.c_int, c.c_uint32]
     L.logo_ctx_set_descent_mode.argtypes = [_vp, c.c_int]
+    L.logo_ctx_set_route_io.argtypes = [_vp, c.c_int]
     L.logo_ctx_stream.restype = _vp
     L.logo_ctx_stream.argtypes = [_vp]
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
@@ -284,6 +289,21 @@ class Solver:
                                    ctypes.byref(st) if stats else None), self._h)
         return r, (st.as_dict() if stats else None)
 
+    def optimize_inplace(self, route, max_moves=0, stats=False):
+        """2-opt descent on `route` itself (a C-contiguous uint32 array of
+        length n, rewritten with the result), as the reference's
+        LocalSolver::optimize(route) works on the caller's buffer: the
+        C-ABI call with no copy on the Python side.  Returns the stats dict
+        or None."""
+        if (not isinstance(route, np.ndarray) or route.dtype != np.uint32 or
+                route.shape != (self.n,) or not route.flags.c_contiguous or
+                not route.flags.writeable):
+            raise ValueError(f"route must be a writeable C-contiguous uint32 array of shape ({self.n},)")
+        st = Stats() if stats else None
+        _check(load().logo_descend(self._h, route.ctypes.data_as(_u32p), max_moves,
+                                   ctypes.byref(st) if stats else None), self._h)
+        return st.as_dict() if stats else None
+
     def optimize_trace(self, route, max_moves=0, trace_cap=1 << 20):
         """Descent that also returns the (minchange, i, j) of every move."""
         r = np.array(route, dtype=np.uint32, copy=True)
@@ -367,6 +387,11 @@ class Solver:
     def set_descent_mode(self, mode):
         """DESCENT_AUTO, DESCENT_GRAPH or DESCENT_COOPERATIVE."""
         _check(load().logo_ctx_set_descent_mode(self._h, mode), self._h)
+
+    def set_route_io(self, mode):
+        """ROUTE_IO_AUTO, ROUTE_IO_COPY or ROUTE_IO_DIRECT (how route buffers
+        reach the device; info()["route_io"] gives the mode in use)."""
+        _check(load().logo_ctx_set_route_io(self._h, mode), self._h)
 
     def set_shape(self, rows_per_thread, warps_per_cta, tile_cols):
         _check(load().logo_ctx_set_shape(self._h, rows_per_thread, warps_per_cta, tile_cols),

@@ -417,6 +417,13 @@ logo_status logo_write_tour(const char *path, const uint32_t *route, uint32_t n,
  * order and mishandles duplicate points). */
 logo_status logo_mf_tour(const logo_xy *coords, uint32_t n, uint32_t *route);
 
+/* The k nearest other cities of every city (1 <= k <= 64): out[v*k + j],
+ * nearest first, by squared distance in double with ties to the lower id;
+ * with fewer than k other cities the remaining slots repeat the last one
+ * found (v itself when n == 1).  The candidate lists of LOGO_SEARCH_NEIGHBOUR
+ * (no reference counterpart). */
+logo_status logo_neighbours(const logo_xy *coords, uint32_t n, uint32_t k, uint32_t *out);
+
 /* Seeded random start tour (routeInit with ROUTE_INIT_SHUFFLE,
  * src/utils/construction.c:129-137, which uses random_shuffle on rand()):
  * Fisher-Yates driven by SplitMix64. */
@@ -443,7 +450,9 @@ typedef struct logo_ctx_info {
     uint64_t host_waits;  /* times this context's calls have waited on the device so far
                              (one logo_ils call: a fixed handful, whatever the kick count) */
     int route_io;         /* LOGO_ROUTE_IO_COPY or LOGO_ROUTE_IO_DIRECT in use */
-    int pad0;
+    int search;           /* LOGO_SEARCH_* */
+    uint32_t search_neighbours; /* neighbour-list length of LOGO_SEARCH_NEIGHBOUR */
+    uint32_t pad0;
 } logo_ctx_info;
 
 logo_status logo_ctx_get_info(const logo_ctx *ctx, logo_ctx_info *info);
@@ -483,6 +492,25 @@ logo_status logo_ctx_set_descent_mode(logo_ctx *ctx, int mode);
 /* INVALID_ARG for an unknown mode, or DIRECT where the device cannot reach
  * pageable host memory. */
 logo_status logo_ctx_set_route_io(logo_ctx *ctx, int mode);
+
+/* Which moves a descent (logo_descend, logo_descend_resident, the descents of
+ * logo_ils) applies.
+ * LOGO_SEARCH_EXHAUSTIVE (default): the best of all (n-2)(n-3)/2 pairs each
+ *   step -- the reference's best improvement (CPUSolver::optimizeStep,
+ *   src/solvers/cpuSolver.cpp:104-146), bit-exact.
+ * LOGO_SEARCH_NEIGHBOUR: first the best of the 2-opt moves that create an
+ *   edge from a city to one of its `neighbours` nearest cities (2 x
+ *   neighbours x n candidate pairs per step, lowest (delta, i, j) first),
+ *   until none improves; then full sweeps as above to a local optimum of
+ *   the whole pair set.  The end point is a 2-opt local optimum, reached
+ *   along another path than the reference's, in far fewer pair evaluations
+ *   at large n (no counterpart in the reference).  Descents in this mode
+ *   always use graph launches (not the cooperative kernel).
+ * neighbours: 1..16, 0 = 8.  INVALID_ARG for an unknown mode or list
+ * length. */
+#define LOGO_SEARCH_EXHAUSTIVE 0
+#define LOGO_SEARCH_NEIGHBOUR 1
+logo_status logo_ctx_set_search(logo_ctx *ctx, int mode, uint32_t neighbours);
 
 /* Sweep kernel variants; all return identical moves (the default depends on
  * n, see logo_ctx_info.variant).

@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblogo_gpu.so")
 SOURCES = ["sweep.cu", "tour.cu", "coop.cu", "capi.cu", "diag.cu", "construct.cpp", "batch.cu",
-           "capi_batch.cu", "noalloc.cu",
+           "capi_batch.cu", "noalloc.cu", "neighbour.cu",
            "serve.cu", "capi_server.cu"]
 # host files whose floating point must not be contracted into FMAs
 NO_CONTRACT = {"construct.cpp"}

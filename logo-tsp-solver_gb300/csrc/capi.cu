@@ -36,6 +36,12 @@ struct logo_ctx {
     uint32_t* d_seen = nullptr;   // route permutation check: last load that met each city
     uint32_t load_epoch = 0;      // loads so far (mod 2^32 - 1, from 1)
     int route_io = LOGO_ROUTE_IO_AUTO;
+    int search = LOGO_SEARCH_EXHAUSTIVE;
+    uint32_t search_k = kSearchNeighbours;  // neighbour-list length of LOGO_SEARCH_NEIGHBOUR
+    uint32_t* d_nbr_search = nullptr;       // search_k nearest cities per city
+    uint32_t nbr_list_k = 0;                // length d_nbr_search was built with
+    cudaGraphExec_t nbr_chunk_exec = nullptr;  // nbr_chunk_steps x (neighbour sweep, apply)
+    uint32_t nbr_chunk_steps = 32;
     bool pageable_ok = false;     // the device reads and writes pageable host memory
     float4* d_wbox = nullptr;     // per-window boxes and largest edges (boxed sweep)
     float* d_wmax = nullptr;
@@ -105,6 +111,20 @@ TourBufs bufs(const logo_ctx* c) {
     return T;
 }
 
+NbrLaunch nbr_args(const logo_ctx* c) {
+    NbrLaunch L;
+    L.Q0 = c->d_Q[0];
+    L.Q1 = c->d_Q[1];
+    L.R0 = c->d_route[0];
+    L.R1 = c->d_route[1];
+    L.pos = c->d_pos;
+    L.nbr = c->d_nbr_search;
+    L.K = c->search_k;
+    L.n = c->n;
+    L.st = c->d_st;
+    return L;
+}
+
 SweepLaunch sweep_args(const logo_ctx* c) {
     SweepLaunch L;
     L.Q0 = c->d_Q[0];
@@ -132,6 +152,13 @@ SweepLaunch sweep_args(const logo_ctx* c) {
 }
 
 uint64_t pairs_of(uint32_t n) { return n < 4 ? 0 : (uint64_t)(n - 2) * (n - 3) / 2; }
+
+// Pairs decided by `sweeps` sweeps of which `nbr` were neighbour sweeps
+// (2K candidate pairs per position).
+uint64_t pair_evals_of(const logo_ctx* c, uint64_t sweeps, uint64_t nbr) {
+    nbr = std::min(nbr, sweeps);
+    return (sweeps - nbr) * pairs_of(c->n) + nbr * 2ull * c->search_k * c->n;
+}
 
 // Default tile shape by size (overridable through logo_ctx_set_shape and
 // logo_ctx_set_kernel).
@@ -203,6 +230,10 @@ logo_status rebuild(logo_ctx* c) {
         cudaGraphExecDestroy(c->chunk_exec);
         c->chunk_exec = nullptr;
     }
+    if (c->nbr_chunk_exec) {
+        cudaGraphExecDestroy(c->nbr_chunk_exec);
+        c->nbr_chunk_exec = nullptr;
+    }
     if (c->ils_exec) {
         cudaGraphExecDestroy(c->ils_exec);
         c->ils_exec = nullptr;
@@ -260,6 +291,52 @@ logo_status rebuild(logo_ctx* c) {
     e = cudaGraphInstantiate(&c->chunk_exec, g, 0);
     cudaGraphDestroy(g);
     CK(c, e);
+    if (c->search == LOGO_SEARCH_NEIGHBOUR) {
+        g = nullptr;
+        CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const NbrLaunch N = nbr_args(c);
+        e = cudaSuccess;
+        for (uint32_t s = 0; s < c->nbr_chunk_steps && e == cudaSuccess; ++s) {
+            e = launch_nbr_sweep(N, c->stream);
+            if (e == cudaSuccess) e = launch_apply_move(T, c->stream);
+        }
+        e2 = cudaStreamEndCapture(c->stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return fail(c, LOGO_ERR_CUDA,
+                        std::string("graph capture: ") +
+                            cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        e = cudaGraphInstantiate(&c->nbr_chunk_exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(c, e);
+    }
+    return LOGO_OK;
+}
+
+// Neighbour lists and exact positions for LOGO_SEARCH_NEIGHBOUR (host grid
+// search, once per list length); graphs are rebuilt by the caller.
+logo_status prepare_search(logo_ctx* c) {
+    if (!c->d_pos) {
+        CK(c, cudaMalloc(&c->d_pos, sizeof(uint32_t) * c->n));
+        CK(c, cudaMemset(c->d_pos, 0, sizeof(uint32_t) * c->n));
+    }
+    if (c->have_route)  // positions were not kept while nothing needed them
+        CK(c, launch_fill_pos(nbr_args(c), c->stream));
+    if (c->nbr_list_k != c->search_k) {
+        std::vector<logo_xy> h(c->n);
+        CK(c, cudaMemcpy(h.data(), c->d_xy, sizeof(logo_xy) * c->n, cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> nb((size_t)c->n * c->search_k);
+        knn_grid(h.data(), c->n, c->search_k, nb.data());
+        if (c->d_nbr_search) cudaFree(c->d_nbr_search);
+        c->d_nbr_search = nullptr;
+        c->nbr_list_k = 0;
+        CK(c, cudaMalloc(&c->d_nbr_search, sizeof(uint32_t) * nb.size()));
+        CK(c, cudaMemcpy(c->d_nbr_search, nb.data(), sizeof(uint32_t) * nb.size(),
+                         cudaMemcpyHostToDevice));
+        c->nbr_list_k = c->search_k;
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
     return LOGO_OK;
 }
 
@@ -311,28 +388,41 @@ cudaError_t capturing_graph(cudaStream_t s, cudaGraph_t* g) {
     return cudaStreamGetCaptureInfo(s, &cst, nullptr, g, nullptr, nullptr, nullptr);
 }
 
-// descent_cond(first) + WHILE(h) { chunk_steps x (sweep, apply) + descent_cond }
-// at the capture position of s (graph g holds the WHILE node); bs captures the body.
-cudaError_t capture_descent_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
-                                 cudaStream_t bs) {
+// descent_cond(first) + WHILE(h) { steps x (sweep, apply) + descent_cond }
+// at the capture position of s (graph g holds the WHILE node); bs captures
+// the body.  nbr: neighbour sweeps instead of full ones.
+cudaError_t capture_sweep_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
+                               cudaStream_t bs, bool nbr) {
     cudaGraphConditionalHandle h;
     cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
     if (e != cudaSuccess) return e;
     e = launch_descent_cond(c->d_st, h, true, s);
     if (e != cudaSuccess) return e;
     const SweepLaunch L = sweep_args(c);
+    const NbrLaunch N = nbr_args(c);
     const TourBufs T = bufs(c);
-    const uint32_t steps = c->chunk_steps;
+    const uint32_t steps = nbr ? c->nbr_chunk_steps : c->chunk_steps;
     DevState* st = c->d_st;
     return capture_while(s, h, bs, [&](cudaStream_t b) {
         cudaError_t eb = cudaSuccess;
         for (uint32_t k = 0; k < steps && eb == cudaSuccess; ++k) {
-            eb = launch_sweep(L, b);
+            eb = nbr ? launch_nbr_sweep(N, b) : launch_sweep(L, b);
             if (eb == cudaSuccess) eb = launch_apply_move(T, b);
         }
         if (eb == cudaSuccess) eb = launch_descent_cond(st, h, false, b);
         return eb;
     });
+}
+
+// One descent at the capture position of s: the full-sweep loop, or with
+// LOGO_SEARCH_NEIGHBOUR the neighbour loop, a resume and the full loop.
+cudaError_t capture_descent_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
+                                 cudaStream_t bs) {
+    if (c->search != LOGO_SEARCH_NEIGHBOUR) return capture_sweep_loop(c, s, g, bs, false);
+    cudaError_t e = capture_sweep_loop(c, s, g, bs, true);
+    if (e == cudaSuccess) e = launch_resume_descent(bufs(c), s);
+    if (e == cudaSuccess) e = capture_sweep_loop(c, s, g, bs, false);
+    return e;
 }
 
 logo_status build_ils_graph(logo_ctx* c) {
@@ -461,8 +551,9 @@ logo_status status_to_error(logo_ctx* c, unsigned int st) {
 
 // Descent on the resident tour.  Replays the chunk graph until the device
 // reports convergence (or the move limit).
-logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0,
-                          uint32_t* route_out, bool* route_stored);
+logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool partial_ok, uint64_t moves0,
+                          uint64_t before, uint32_t* route_out, bool* route_stored,
+                          bool nbr = false);
 logo_status enqueue_route_out(logo_ctx* c, uint32_t* route, bool best);
 
 // Cooperative descents of this library never overlap on one device: each
@@ -475,7 +566,8 @@ std::mutex& coop_lock(int device) {
 }
 
 bool use_coop(const logo_ctx* c) {
-    return c->coop_grid > 0 && c->descent_mode != LOGO_DESCENT_GRAPH;
+    return c->coop_grid > 0 && c->descent_mode != LOGO_DESCENT_GRAPH &&
+           c->search == LOGO_SEARCH_EXHAUSTIVE;
 }
 
 // reset_enqueued: the reset was folded into the route load just before.
@@ -527,8 +619,20 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
         if (s != LOGO_OK) return s;
         if (!c->h_st->converged && !c->h_st->status)
             return fail(c, LOGO_ERR_DEVICE_FAULT, "cooperative descent did not finish");
+    } else if (c->search == LOGO_SEARCH_NEIGHBOUR) {
+        // neighbour sweeps until no candidate improves, then full sweeps
+        logo_status s = graph_descent(c, max_moves, reset, moves0, moves0, nullptr, nullptr,
+                                      true);
+        if (s != LOGO_OK) return s;
+        if (!c->h_st->status && !c->h_st->bad_route) {
+            CK(c, launch_resume_descent(bufs(c), c->stream));
+            s = graph_descent(c, max_moves, reset, moves0, c->h_st->moves, route_out,
+                              route_stored);
+            if (s != LOGO_OK) return s;
+        }
     } else {
-        logo_status s = graph_descent(c, max_moves, reset, moves0, route_out, route_stored);
+        logo_status s = graph_descent(c, max_moves, reset, moves0, moves0, route_out,
+                                      route_stored);
         if (s != LOGO_OK) return s;
     }
     if (moves_out) *moves_out = c->h_st->moves - moves0;
@@ -541,19 +645,21 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
 
 // Replays the chunk graph (or single steps when fewer moves are allowed than
 // a chunk holds) until the device flags convergence.
-logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t moves0,
-                          uint32_t* route_out, bool* route_stored) {
-    uint64_t before = moves0;
+logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool partial_ok, uint64_t moves0,
+                          uint64_t before, uint32_t* route_out, bool* route_stored, bool nbr) {
+    const uint32_t chunk = nbr ? c->nbr_chunk_steps : c->chunk_steps;
     for (;;) {
         const uint64_t left = max_moves - (before - moves0);
         bool stored = false;
-        if (reset && left < c->chunk_steps) {
+        if (partial_ok && left < chunk) {
             // fewer moves allowed than a chunk holds: launch just those steps,
-            // after which the descent has converged or met its move limit
+            // after which the descent (or its neighbour phase) has converged
+            // or met its move limit
             const SweepLaunch L = sweep_args(c);
+            const NbrLaunch N = nbr_args(c);
             const TourBufs T = bufs(c);
             for (uint64_t k = 0; k < left; ++k) {
-                CK(c, launch_sweep(L, c->stream));
+                CK(c, nbr ? launch_nbr_sweep(N, c->stream) : launch_sweep(L, c->stream));
                 CK(c, launch_apply_move(T, c->stream));
             }
             if (route_out) {
@@ -562,7 +668,7 @@ logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool reset, uint64_t 
                 stored = true;
             }
         } else {
-            CK(c, cudaGraphLaunch(c->chunk_exec, c->stream));
+            CK(c, cudaGraphLaunch(nbr ? c->nbr_chunk_exec : c->chunk_exec, c->stream));
         }
         logo_status s = read_state(c);
         if (s != LOGO_OK) return s;
@@ -632,6 +738,8 @@ void destroy(logo_ctx* c) {
     cudaFree(c->d_workctl);
     cudaFree(c->d_pos);
     cudaFree(c->d_nbr);
+    cudaFree(c->d_nbr_search);
+    if (c->nbr_chunk_exec) cudaGraphExecDestroy(c->nbr_chunk_exec);
     cudaFree(c->d_coop);
     if (c->h_st) cudaFreeHost(c->h_st);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -801,8 +909,31 @@ logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
     info->cooperative_ctas = c->coop_grid;
     info->host_waits = c->host_waits;
     info->route_io = route_direct(c) ? LOGO_ROUTE_IO_DIRECT : LOGO_ROUTE_IO_COPY;
+    info->search = c->search;
+    info->search_neighbours = c->search_k;
     info->pad0 = 0;
     return LOGO_OK;
+}
+
+logo_status logo_ctx_set_search(logo_ctx* c, int mode, uint32_t neighbours) {
+    if (!c) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
+    if (mode != LOGO_SEARCH_EXHAUSTIVE && mode != LOGO_SEARCH_NEIGHBOUR)
+        return fail(c, LOGO_ERR_INVALID_ARG, "unknown search mode");
+    if (neighbours == 0) neighbours = kSearchNeighbours;
+    if (neighbours > kSearchNeighboursMax)
+        return fail(c, LOGO_ERR_INVALID_ARG,
+                    "neighbour lists hold at most " + std::to_string(kSearchNeighboursMax) +
+                        " cities");
+    CK(c, cudaSetDevice(c->device));
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->search = mode;
+    c->search_k = neighbours;
+    if (mode == LOGO_SEARCH_NEIGHBOUR) {
+        logo_status s = prepare_search(c);
+        if (s != LOGO_OK) return s;
+    }
+    return rebuild(c);
 }
 
 logo_status logo_ctx_set_route_io(logo_ctx* c, int mode) {
@@ -996,7 +1127,7 @@ logo_status logo_descend_resident(logo_ctx* c, uint64_t max_moves, logo_stats* s
         std::memset(stats, 0, sizeof(*stats));
         stats->moves = moves;
         stats->sweeps = sweeps;
-        stats->pair_evals = sweeps * pairs_of(c->n);
+        stats->pair_evals = pair_evals_of(c, sweeps, c->h_st->nbr_sweeps);
         stats->descents = 1;
         stats->device_ms = ms;
     }
@@ -1050,6 +1181,7 @@ static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves
     bool stored = false;
     s = run_descent(c, max_moves, &moves, &sweeps, true, quick,
                     quick && route_direct(c) ? route : nullptr, &stored);
+    const uint64_t nbr_sweeps = c->h_st->nbr_sweeps;
     if (d_log) {
         int* null_log = nullptr;
         const unsigned int zero = 0;
@@ -1077,7 +1209,7 @@ static logo_status descend_impl(logo_ctx* c, uint32_t* route, uint64_t max_moves
         std::memset(stats, 0, sizeof(*stats));
         stats->moves = moves;
         stats->sweeps = sweeps;
-        stats->pair_evals = sweeps * pairs_of(c->n);
+        stats->pair_evals = pair_evals_of(c, sweeps, nbr_sweeps);
         stats->descents = 1;
         stats->start_length = start_len;
         stats->final_length = final_len;
@@ -1168,7 +1300,7 @@ logo_status logo_ils(logo_ctx* c, uint32_t* route, uint32_t kicks, uint64_t seed
         std::memset(stats, 0, sizeof(*stats));
         stats->moves = fin.total_moves;
         stats->sweeps = fin.sweeps;
-        stats->pair_evals = fin.sweeps * pairs_of(c->n);
+        stats->pair_evals = pair_evals_of(c, fin.sweeps, fin.nbr_sweeps);
         stats->descents = (uint64_t)kicks + 1;
         stats->kicks = fin.kicks;
         stats->accepted = fin.accepted;

@@ -269,11 +269,13 @@ namespace logo {
 
 // k nearest other cities of every city (by squared double distance, ties to
 // the lower id), written as out[v * k + j], nearest first; fewer than k
-// other cities leave the remaining slots at the nearest one found (or v
-// itself when n == 1).  A uniform grid of about two cities per cell; each
-// query scans square rings of cells until k candidates are held and the
-// next ring is farther than the k-th.  Used only to seed the sweep's bound
-// with near-neighbour pairs, so any valid neighbour set keeps results exact.
+// other cities leave the remaining slots at the last one found (or v itself
+// when n == 1).  A uniform grid of about two cities per cell; each query
+// scans square rings of cells until k candidates are held and the next ring
+// is farther than the k-th (with a relative allowance for the rounding of
+// the cell arithmetic, so the lists are exact).  The boxed sweep seeds its
+// bound with these pairs (any list keeps its results exact); the neighbour
+// search (LOGO_SEARCH_NEIGHBOUR) takes its candidate moves from them.
 void knn_grid(const logo_xy* p, uint32_t n, uint32_t k, uint32_t* out) {
     if (n == 0 || k == 0) return;
     double x0 = p[0].x, x1 = p[0].x, y0 = p[0].y, y1 = p[0].y;
@@ -334,7 +336,7 @@ void knn_grid(const logo_xy* p, uint32_t n, uint32_t k, uint32_t* out) {
                 }
             }
             // every unscanned city is at least r cells away on one axis
-            const double reach = r * std::min(cw, ch);
+            const double reach = r * std::min(cw, ch) * (1.0 - 1e-9);
             if (best.size() == k && reach * reach > best.back().first) break;
             if (r > (int)(gw + gh)) break;
         }
@@ -363,6 +365,14 @@ logo_status logo_nn_tour(const logo_xy* coords, uint32_t n, uint32_t start, uint
         px = coords[id].x;
         py = coords[id].y;
     }
+    return LOGO_OK;
+}
+
+logo_status logo_neighbours(const logo_xy* coords, uint32_t n, uint32_t k, uint32_t* out) {
+    if (!coords || !out || n == 0 || n > LOGO_MAX_CITIES || k == 0 || k > 64)
+        return LOGO_ERR_INVALID_ARG;
+    if (!finite_coords(coords, n)) return LOGO_ERR_INVALID_ARG;
+    logo::knn_grid(coords, n, k, out);
     return LOGO_OK;
 }
 

@@ -68,6 +68,7 @@ struct DevState {
     unsigned long long start_length; // length of the tour the call started from
     unsigned int kick_kind;         // LOGO_KICK_SEGMENT or LOGO_KICK_DOUBLE_BRIDGE
     unsigned int load_bad;          // set by a CTA of load_route_kernel that met a bad id
+    unsigned long long nbr_sweeps;  // neighbour sweeps of this descent (or ILS call)
 };
 
 __host__ __device__ __forceinline__ uint64_t pack_key(int delta, uint32_t i,

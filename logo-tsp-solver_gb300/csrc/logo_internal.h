@@ -62,6 +62,26 @@ cudaError_t launch_sweep_prepare(const SweepLaunch& L);
 bool sweep_shape_supported(int R, int NW, int variant);
 size_t sweep_smem_bytes(uint32_t cb);
 
+// ---- neighbour-list search (neighbour.cu) ------------------------------------
+struct NbrLaunch {
+    const OrderedCity* Q0;
+    const OrderedCity* Q1;
+    const uint32_t* R0;
+    const uint32_t* R1;
+    uint32_t* pos;        // tour position of every city (exact: kept by every tour move)
+    const uint32_t* nbr;  // K nearest other cities per city, nearest first
+    uint32_t K;
+    uint32_t n;
+    DevState* st;
+};
+// Default and largest neighbour-list length of LOGO_SEARCH_NEIGHBOUR.
+constexpr uint32_t kSearchNeighbours = 8, kSearchNeighboursMax = 16;
+// One neighbour sweep: the lowest improving candidate key into st->best_key
+// (the apply kernel then moves or marks convergence), st->nbr_sweeps += 1.
+cudaError_t launch_nbr_sweep(const NbrLaunch& L, cudaStream_t s);
+// Recomputes pos from the current tour.
+cudaError_t launch_fill_pos(const NbrLaunch& L, cudaStream_t s);
+
 // ---- tour maintenance (tour.cu) --------------------------------------------
 struct TourBufs {
     OrderedCity* Q[2];
@@ -129,6 +149,9 @@ cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves
                                  cudaStream_t s);
 // Applies the move in st->best_key (or marks convergence).
 cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s);
+// After a converged neighbour phase: continue the same descent (moves and
+// limit kept) with full sweeps, unless it stopped on an error or the limit.
+cudaError_t launch_resume_descent(const TourBufs& T, cudaStream_t s);
 // st->length = length of the current tour.
 cudaError_t launch_tour_length(const TourBufs& T, cudaStream_t s);
 // ILS pieces.

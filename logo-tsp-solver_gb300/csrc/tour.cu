@@ -90,6 +90,7 @@ __global__ void load_route_kernel(const float2* __restrict__ xy, const uint32_t*
         if (reset_moves) {
             st->best_key = kNoMove;
             st->moves = 0;
+            st->nbr_sweeps = 0;
             st->status = 0u;
             st->converged = b ? 1u : 0u;
             st->sweeps_at_reset = st->sweeps;
@@ -113,6 +114,7 @@ __global__ void store_route_kernel(const uint32_t* __restrict__ R0,
 __global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves) {
     st->best_key = kNoMove;
     st->moves = 0;
+    st->nbr_sweeps = 0;
     st->status = 0u;
     st->converged = st->bad_route ? 1u : 0u;  // nothing to descend on a bad route
     st->sweeps_at_reset = st->sweeps;
@@ -359,6 +361,19 @@ cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves
     reset_descent_kernel<<<1, 1, 0, s>>>(T.st, max_moves);
     return cudaGetLastError();
 }
+__global__ void resume_descent_kernel(DevState* st) {
+    const unsigned int bad = st->status | st->bad_route;  // includes the move limit
+    if (!bad) {
+        st->converged = 0u;
+        st->best_key = kNoMove;
+    }
+}
+
+cudaError_t launch_resume_descent(const TourBufs& T, cudaStream_t s) {
+    resume_descent_kernel<<<1, 1, 0, s>>>(T.st);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s) {
     apply_move_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);
     return cudaGetLastError();

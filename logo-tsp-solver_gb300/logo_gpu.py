@@ -31,6 +31,8 @@ DESCENT_COOPERATIVE = 2
 ROUTE_IO_AUTO = 0
 ROUTE_IO_COPY = 1
 ROUTE_IO_DIRECT = 2
+SEARCH_EXHAUSTIVE = 0
+SEARCH_NEIGHBOUR = 1
 START_GIVEN = 0
 START_NN = 1
 START_MF = 2
@@ -54,7 +56,8 @@ EXPORTS = [
     "logo_best_move_noalloc", "logo_ctx_set_kernel", "logo_ctx_set_descent_mode",
     "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
     "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
-    "logo_diag_flag_timeout", "logo_ctx_set_route_io",
+    "logo_diag_flag_timeout", "logo_ctx_set_route_io", "logo_ctx_set_search",
+    "logo_neighbours",
 ]
 
 
@@ -87,7 +90,8 @@ class CtxInfo(ctypes.Structure):
                 ("filter_margin", ctypes.c_float), ("graph_steps", ctypes.c_uint32),
                 ("variant", ctypes.c_int), ("descent_mode", ctypes.c_int),
                 ("cooperative_ctas", ctypes.c_int), ("host_waits", ctypes.c_uint64),
-                ("route_io", ctypes.c_int), ("pad0", ctypes.c_int)]
+                ("route_io", ctypes.c_int), ("search", ctypes.c_int),
+                ("search_neighbours", ctypes.c_uint32), ("pad0", ctypes.c_uint32)]
 
 
 class Instance(ctypes.Structure):
@@ -179,6 +183,7 @@ def load(path=LIB_PATH):
     L.logo_ctx_set_kernel.argtypes = [_vp, c.c_int, c.c_int, c.c_int, c.c_uint32]
     L.logo_ctx_set_descent_mode.argtypes = [_vp, c.c_int]
     L.logo_ctx_set_route_io.argtypes = [_vp, c.c_int]
+    L.logo_ctx_set_search.argtypes = [_vp, c.c_int, c.c_uint32]
     L.logo_ctx_stream.restype = _vp
     L.logo_ctx_stream.argtypes = [_vp]
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
@@ -195,6 +200,7 @@ def load(path=LIB_PATH):
     L.logo_read_tsplib.argtypes = [c.c_char_p, _vp, c.c_uint32, _u32p]
     L.logo_nn_tour.argtypes = [_vp, c.c_uint32, c.c_uint32, _u32p]
     L.logo_mf_tour.argtypes = [_vp, c.c_uint32, _u32p]
+    L.logo_neighbours.argtypes = [_vp, c.c_uint32, c.c_uint32, _u32p]
     L.logo_tsplib_info.argtypes = [c.c_char_p, _u32p, c.POINTER(c.c_int)]
     L.logo_read_tour.argtypes = [c.c_char_p, _u32p, c.c_uint32, _u32p]
     L.logo_write_tour.argtypes = [c.c_char_p, _u32p, c.c_uint32, c.c_char_p, c.c_int]
@@ -393,6 +399,12 @@ class Solver:
         reach the device; info()["route_io"] gives the mode in use)."""
         _check(load().logo_ctx_set_route_io(self._h, mode), self._h)
 
+    def set_search(self, mode, neighbours=0):
+        """SEARCH_EXHAUSTIVE (the reference's best improvement) or
+        SEARCH_NEIGHBOUR (neighbour-list moves first, then full sweeps to a
+        2-opt local optimum); neighbours 1..16, 0 = 8."""
+        _check(load().logo_ctx_set_search(self._h, mode, neighbours), self._h)
+
     def set_shape(self, rows_per_thread, warps_per_cta, tile_cols):
         _check(load().logo_ctx_set_shape(self._h, rows_per_thread, warps_per_cta, tile_cols),
                self._h)
@@ -423,6 +435,15 @@ def nn_tour(coords, start=0):
     r = np.zeros(len(xy), dtype=np.uint32)
     _check(load().logo_nn_tour(xy.ctypes.data, len(xy), start, r.ctypes.data_as(_u32p)))
     return r
+
+
+def neighbours(coords, k):
+    """(n, k) uint32: the k nearest other cities of every city (the
+    candidate lists of SEARCH_NEIGHBOUR; host only)."""
+    xy = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 2)
+    out = np.zeros((len(xy), k), dtype=np.uint32)
+    _check(load().logo_neighbours(xy.ctypes.data, len(xy), k, out.ctypes.data_as(_u32p)))
+    return out
 
 
 def mf_tour(coords):

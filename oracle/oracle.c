@@ -332,9 +332,17 @@ uint64_t lo_tour_length(const float *xy, const uint32_t *route, uint32_t n)
 
 /* src/solvers/twoOptLocalSolver.cpp:22-64; each sweep on `threads` pthreads
  * (the same move: the parallel sweep keeps the lowest-(delta, i, j) rule). */
+static uint64_t nbr_sweep(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
+                          const uint32_t *nbr, uint32_t k);
+
+/* With nbr (k cities per city), the neighbour phase of LOGO_SEARCH_NEIGHBOUR
+ * comes first: moves from nbr_sweep until none improves, then the full
+ * sweeps below; both count towards max_moves (and *nbr_moves gets the
+ * first phase's count). */
 static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
                             uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
-                            int threads)
+                            int threads, const uint32_t *nbr, uint32_t k,
+                            uint64_t *nbr_moves)
 {
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
     int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(n + 1));
@@ -344,7 +352,42 @@ static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
     o.y = (float *)malloc(sizeof(float) * (n + 1));
     o.e = (int32_t *)malloc(sizeof(int32_t) * (n + 1));
     o.n = n;
-    for (;;) {
+    if (nbr_moves)
+        *nbr_moves = 0;
+    if (nbr && k) {
+        uint32_t *pos = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
+        for (;;) {
+            for (uint32_t q = 0; q < n; q++) {
+                o.x[q] = xy[2 * (size_t)route[q]];
+                o.y[q] = xy[2 * (size_t)route[q] + 1];
+                pos[route[q]] = q;
+            }
+            for (uint32_t q = 1; q < n; q++)
+                o.e[q] = lo_dist(o.x[q - 1], o.y[q - 1], o.x[q], o.y[q]);
+            o.e[0] = lo_dist(o.x[n - 1], o.y[n - 1], o.x[0], o.y[0]);
+            uint64_t key = nbr_sweep(&o, route, pos, nbr, k);
+            if (key == UINT64_MAX)
+                break;
+            if ((uint64_t)moves >= max_moves) {
+                moves = -1;
+                break;
+            }
+            int32_t d;
+            uint32_t i, j;
+            unpack_key(key, &d, &i, &j);
+            if (move_log && (uint64_t)moves < log_cap) {
+                move_log[3 * moves + 0] = d;
+                move_log[3 * moves + 1] = (int32_t)i;
+                move_log[3 * moves + 2] = (int32_t)j;
+            }
+            lo_apply_move(route, n, i, j, tmp);
+            moves++;
+        }
+        free(pos);
+        if (nbr_moves && moves >= 0)
+            *nbr_moves = (uint64_t)moves;
+    }
+    while (moves >= 0) {
         for (uint32_t k = 0; k < n; k++) {
             o.x[k] = xy[2 * (size_t)route[k]];
             o.y[k] = xy[2 * (size_t)route[k] + 1];
@@ -382,14 +425,111 @@ static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
 int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
                    uint64_t max_moves, int32_t *move_log, uint64_t log_cap)
 {
-    return descend_impl(xy, route, n, max_moves, move_log, log_cap, 1);
+    return descend_impl(xy, route, n, max_moves, move_log, log_cap, 1, NULL, 0, NULL);
 }
 
 int64_t lo_descend_mt(const float *xy, uint32_t *route, uint32_t n,
                       uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
                       int threads)
 {
-    return descend_impl(xy, route, n, max_moves, move_log, log_cap, threads);
+    return descend_impl(xy, route, n, max_moves, move_log, log_cap, threads, NULL, 0, NULL);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Neighbour-list search (LOGO_SEARCH_NEIGHBOUR; no reference counterpart)    */
+/* ------------------------------------------------------------------------ */
+
+/* k nearest other cities of every city by squared distance in double
+ * (dx = (double)x_v - (double)x_u, dx*dx + dy*dy), ties to the lower id,
+ * out[v*k + j] nearest first; with fewer than k other cities the remaining
+ * slots repeat the last one found (v itself when there is none).  Brute
+ * force over all pairs: the test sizes only. */
+int lo_knn(const float *xy, uint32_t n, uint32_t k, uint32_t *out)
+{
+    double *bd = (double *)malloc(sizeof(double) * (k + 1));
+    uint32_t *bi = (uint32_t *)malloc(sizeof(uint32_t) * (k + 1));
+    if (!bd || !bi) {
+        free(bd);
+        free(bi);
+        return -1;
+    }
+    for (uint32_t v = 0; v < n; v++) {
+        const double px = xy[2 * (size_t)v], py = xy[2 * (size_t)v + 1];
+        uint32_t cnt = 0;
+        for (uint32_t u = 0; u < n; u++) {
+            if (u == v)
+                continue;
+            const double dx = px - (double)xy[2 * (size_t)u];
+            const double dy = py - (double)xy[2 * (size_t)u + 1];
+            const double d = dx * dx + dy * dy;
+            if (cnt == k && !(d < bd[k - 1] || (d == bd[k - 1] && u < bi[k - 1])))
+                continue;
+            uint32_t at = cnt < k ? cnt : k - 1;
+            while (at > 0 && (d < bd[at - 1] || (d == bd[at - 1] && u < bi[at - 1]))) {
+                bd[at] = bd[at - 1];
+                bi[at] = bi[at - 1];
+                at--;
+            }
+            bd[at] = d;
+            bi[at] = u;
+            if (cnt < k)
+                cnt++;
+        }
+        for (uint32_t j = 0; j < k; j++)
+            out[(size_t)v * k + j] = cnt == 0 ? v : bi[j < cnt ? j : cnt - 1];
+    }
+    free(bd);
+    free(bi);
+    return 0;
+}
+
+/* The candidate pairs of one neighbour sweep: for position i (city route[i])
+ * and each listed neighbour at position p, (a, b) = (min, max) of (i, p),
+ * b >= a + 2: pair (a, b) if a >= 1 and pair (a + 1, b + 1) if
+ * b + 1 <= n - 1, i.e. the two full-sweep pairs whose move creates the edge
+ * between the two cities.  Lowest improving (delta, i, c) key. */
+static uint64_t nbr_sweep(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
+                          const uint32_t *nbr, uint32_t k)
+{
+    const uint32_t n = o->n;
+    const float *X = o->x, *Y = o->y;
+    const int32_t *E = o->e;
+    uint64_t best = UINT64_MAX;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t t = route[i];
+        for (uint32_t q = 0; q < k; q++) {
+            const uint32_t p = pos[nbr[(size_t)t * k + q]];
+            const uint32_t a = i < p ? i : p, b = i < p ? p : i;
+            if (b < a + 2)
+                continue;
+            const int32_t D = lo_dist(X[a], Y[a], X[b], Y[b]);
+            if (a >= 1) {
+                const int32_t delta = D + lo_dist(X[a - 1], Y[a - 1], X[b - 1], Y[b - 1]) -
+                                      E[a] - E[b];
+                if (delta < 0) {
+                    const uint64_t key = lo_pack_key(delta, a, b);
+                    if (key < best)
+                        best = key;
+                }
+            }
+            if (b + 1 <= n - 1) {
+                const int32_t delta = lo_dist(X[a + 1], Y[a + 1], X[b + 1], Y[b + 1]) + D -
+                                      E[a + 1] - E[b + 1];
+                if (delta < 0) {
+                    const uint64_t key = lo_pack_key(delta, a + 1, b + 1);
+                    if (key < best)
+                        best = key;
+                }
+            }
+        }
+    }
+    return best;
+}
+
+int64_t lo_descend_nbr(const float *xy, uint32_t *route, uint32_t n, const uint32_t *nbr,
+                       uint32_t k, uint64_t max_moves, int threads, uint64_t *nbr_moves)
+{
+    return descend_impl(xy, route, n, max_moves, NULL, 0, threads, nbr, k, nbr_moves);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -434,7 +574,7 @@ void lo_kick_double_bridge(uint32_t *route, uint32_t n, uint64_t *rng,
  * :98-99, and ends after one pass otherwise). */
 static int ils_impl(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
                     uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
-                    lo_ils_stats *stats, int threads)
+                    lo_ils_stats *stats, int threads, const uint32_t *nbr, uint32_t k)
 {
     uint32_t *best = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
@@ -446,7 +586,8 @@ static int ils_impl(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks
     uint64_t best_len = st.start_length;
     memcpy(best, route, sizeof(uint32_t) * n);
     for (uint32_t it = 0;; it++) {
-        int64_t m = descend_impl(xy, route, n, max_moves_per_descent, NULL, 0, threads);
+        int64_t m = descend_impl(xy, route, n, max_moves_per_descent, NULL, 0, threads, nbr, k,
+                                 NULL);
         st.descents++;
         if (m < 0) {
             rc = -1;
@@ -481,7 +622,8 @@ int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
            uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
            lo_ils_stats *stats)
 {
-    return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats, 1);
+    return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats, 1,
+                    NULL, 0);
 }
 
 int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
@@ -489,7 +631,15 @@ int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
               lo_ils_stats *stats, int threads)
 {
     return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats,
-                    threads);
+                    threads, NULL, 0);
+}
+
+int lo_ils_nbr(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks, uint64_t seed,
+               int kick_kind, uint64_t max_moves_per_descent, lo_ils_stats *stats,
+               int threads, const uint32_t *nbr, uint32_t k)
+{
+    return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats,
+                    threads, nbr, k);
 }
 
 /* ------------------------------------------------------------------------ */

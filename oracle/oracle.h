@@ -125,6 +125,22 @@ int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
               uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
               lo_ils_stats *stats, int threads);
 
+/* Neighbour-list search (LOGO_SEARCH_NEIGHBOUR; no reference counterpart):
+ * lo_knn writes the k nearest other cities of every city (squared double
+ * distance, lower id on ties, out[v*k + j] nearest first; fewer than k other
+ * cities repeat the last one found, or v itself).  lo_descend_nbr first
+ * applies the best improving move among the pairs that create an edge from
+ * a city to one of its listed neighbours until none improves, then full
+ * best-improvement sweeps (as lo_descend) to a local optimum; moves of both
+ * phases count towards max_moves, *nbr_moves gets the first phase's.
+ * lo_ils_nbr is lo_ils_mt with those descents. */
+int lo_knn(const float *xy, uint32_t n, uint32_t k, uint32_t *out);
+int64_t lo_descend_nbr(const float *xy, uint32_t *route, uint32_t n, const uint32_t *nbr,
+                       uint32_t k, uint64_t max_moves, int threads, uint64_t *nbr_moves);
+int lo_ils_nbr(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks, uint64_t seed,
+               int kick_kind, uint64_t max_moves_per_descent, lo_ils_stats *stats,
+               int threads, const uint32_t *nbr, uint32_t k);
+
 /* Nearest-neighbour start tour, initRoute_KD_NN
  * (src/utils/kdtree_utils.c:279-301): start at city 0, repeatedly go to the
  * nearest unvisited city by squared distance in double; ties go to the lowest

@@ -84,6 +84,16 @@ def lib():
         L.lo_nn_tour.argtypes = [_f32p, ctypes.c_uint32, _u32p]
         L.lo_check_tour.restype = ctypes.c_int
         L.lo_check_tour.argtypes = [_u32p, ctypes.c_uint32]
+        L.lo_knn.restype = ctypes.c_int
+        L.lo_knn.argtypes = [_f32p, ctypes.c_uint32, ctypes.c_uint32, _u32p]
+        L.lo_descend_nbr.restype = ctypes.c_int64
+        L.lo_descend_nbr.argtypes = [_f32p, _u32p, ctypes.c_uint32, _u32p, ctypes.c_uint32,
+                                     ctypes.c_uint64, ctypes.c_int, _u64p]
+        L.lo_ils_nbr.restype = ctypes.c_int
+        L.lo_ils_nbr.argtypes = [_f32p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                 ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
+                                 ctypes.POINTER(IlsStats), ctypes.c_int, _u32p,
+                                 ctypes.c_uint32]
         L.lo_ils_batch.restype = ctypes.c_int
         L.lo_ils_batch.argtypes = [_f32p, _u32p, _u64p, _u32p, _u64p, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
@@ -149,6 +159,54 @@ def tour_length(xy, route):
     xy, pxy = _f32(xy)
     route, pr = _u32(route)
     return lib().lo_tour_length(pxy, pr, len(route))
+
+
+def knn(xy, k):
+    """(n, k) uint32: the k nearest other cities of every city (squared
+    double distance, lower id on ties; brute force)."""
+    xy, pxy = _f32(xy)
+    n = len(xy)
+    out = np.zeros((n, k), dtype=np.uint32)
+    if lib().lo_knn(pxy, n, k, out.ctypes.data_as(_u32p)):
+        raise MemoryError("oracle knn allocation failed")
+    return out
+
+
+def descend_nbr(xy, route, k=8, max_moves=None, threads=1, stop_at_limit=False):
+    """Neighbour-list search (neighbour moves, then full sweeps): returns
+    (final_route, moves, moves of the neighbour phase).  stop_at_limit: a
+    descent that still has moves after max_moves returns its state there
+    (moves = max_moves) instead of raising."""
+    nb = np.ascontiguousarray(knn(xy, k))
+    xy, pxy = _f32(xy)
+    r = np.array(route, dtype=np.uint32, copy=True)
+    n = len(r)
+    if max_moves is None:
+        max_moves = 64 * n * n + 1024
+    nm = ctypes.c_uint64(0)
+    m = lib().lo_descend_nbr(pxy, r.ctypes.data_as(_u32p), n, nb.ctypes.data_as(_u32p), k,
+                             max_moves, max(1, int(threads)), ctypes.byref(nm))
+    if m < 0:
+        if not stop_at_limit:
+            raise RuntimeError("oracle descent exceeded max_moves")
+        m = max_moves
+    return r, m, nm.value
+
+
+def ils_nbr(xy, route, kicks, seed, kind=KICK_SEGMENT, k=8, max_moves=None, threads=1):
+    """ils() with the neighbour-list search in every descent."""
+    nb = np.ascontiguousarray(knn(xy, k))
+    xy, pxy = _f32(xy)
+    r = np.array(route, dtype=np.uint32, copy=True)
+    n = len(r)
+    if max_moves is None:
+        max_moves = 64 * n * n + 1024
+    st = IlsStats()
+    rc = lib().lo_ils_nbr(pxy, r.ctypes.data_as(_u32p), n, kicks, seed, kind, max_moves,
+                          ctypes.byref(st), max(1, int(threads)), nb.ctypes.data_as(_u32p), k)
+    if rc:
+        raise RuntimeError("oracle ILS descent exceeded max_moves")
+    return r, {f: getattr(st, f) for f, _ in IlsStats._fields_}
 
 
 def descend(xy, route, max_moves=None, log_cap=0, threads=1):

@@ -1,0 +1,115 @@
+"""The neighbour-list search (LOGO_SEARCH_NEIGHBOUR) on the device against
+the oracle's restatement of it (oracle/oracle.c, lo_descend_nbr / lo_ils_nbr,
+whose candidate enumeration is pinned to the exhaustive oracle by
+tests/test_neighbour_search.py).
+
+* Descents: final tour, move count and the neighbour phase's moves equal
+  the oracle's, on uniform, clustered and integer-grid instances (equal
+  distances, duplicate points), from random and nearest-neighbour tours,
+  with the MUFU screen (n = 1000, 5000) and the boxed screen (n = 24,000)
+  finishing the descent, and with lists of 4, 8 and 16 cities.
+* With lists of every other city (n = 17, k = 16) the search is the
+  reference's exhaustive descent, move for move.
+* A move limit stops the search where the oracle's stops.
+* ILS in neighbour mode (segment and double-bridge kicks, the device-run
+  ILS graph) equals the oracle's ILS with the same descents.
+* Switching a context back to the exhaustive search gives the reference's
+  descent again.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 4
+
+
+def _case(lg, inst, kind, n, seed):
+    if kind == "uniform":
+        xy = inst.uniform_f32(n, seed, 1.0e6)
+    elif kind == "clustered":
+        xy = inst.clustered(n, seed, side=1.0e6, clusters=max(2, n // 250))
+    else:
+        xy = np.floor(inst.uniform_int(n, seed) / 40.0).astype(np.float32)
+    r = inst.random_tour(n, seed) if seed % 2 else lg.nn_tour(xy, 0)
+    return xy, r
+
+
+@pytest.mark.parametrize("kind,n,seed,k", [
+    ("uniform", 1000, 1, 8), ("clustered", 1000, 2, 4), ("grid", 1000, 3, 16),
+    ("uniform", 5000, 4, 8), ("grid", 5000, 5, 8), ("clustered", 24000, 6, 8),
+    ("uniform", 24000, 7, 8),
+])
+def test_descent_matches_the_oracle(lg, inst, oracle_mod, kind, n, seed, k):
+    xy, r = _case(lg, inst, kind, n, seed)
+    want, m, nm = oracle_mod.descend_nbr(xy, r, k=k, threads=THREADS)
+    with lg.Solver(xy) as s:
+        s.set_search(lg.SEARCH_NEIGHBOUR, k)
+        info = s.info()
+        assert info["search"] == lg.SEARCH_NEIGHBOUR and info["search_neighbours"] == k
+        got, st = s.optimize(r)
+        assert st["moves"] == m
+        assert st["final_length"] == oracle_mod.tour_length(xy, want)
+        assert np.array_equal(got, want)
+        # fewer pairs than full sweeps would decide
+        assert st["pair_evals"] < st["sweeps"] * (n - 2) * (n - 3) // 2
+        # the same from a resident tour, and with the C-ABI in place
+        s.set_route(r)
+        assert s.descend_resident()["moves"] == m
+        assert np.array_equal(s.get_route(), want)
+        buf = r.copy()
+        s.optimize_inplace(buf)
+        assert np.array_equal(buf, want)
+    assert nm > 0
+
+
+def test_full_lists_are_the_exhaustive_descent(lg, inst, oracle_mod):
+    n = 17
+    for seed in range(4):
+        xy = inst.uniform_int(n, 60 + seed)
+        r = inst.random_tour(n, 60 + seed)
+        want, m, _ = oracle_mod.descend(xy, r)
+        with lg.Solver(xy) as s:
+            s.set_search(lg.SEARCH_NEIGHBOUR, 16)
+            got, st = s.optimize(r)
+        assert np.array_equal(got, want) and st["moves"] == m
+
+
+@pytest.mark.parametrize("limit", [1, 7, 40])
+def test_move_limit(lg, inst, oracle_mod, limit):
+    xy, r = _case(lg, inst, "uniform", 3000, 11)
+    want, m, _ = oracle_mod.descend_nbr(xy, r, k=8, max_moves=limit, threads=THREADS,
+                                       stop_at_limit=True)
+    with lg.Solver(xy) as s:
+        s.set_search(lg.SEARCH_NEIGHBOUR)
+        got, st = s.optimize(r, max_moves=limit)
+    assert st["moves"] == m == limit
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("n,kicks,kind", [(2000, 12, 1), (3000, 8, 0), (20000, 4, 1)])
+def test_ils_matches_the_oracle(lg, inst, oracle_mod, n, kicks, kind):
+    xy, r = _case(lg, inst, "clustered", n, 20 + n)
+    want, wst = oracle_mod.ils_nbr(xy, r, kicks, 5, kind, k=8, threads=THREADS)
+    with lg.Solver(xy) as s:
+        s.set_search(lg.SEARCH_NEIGHBOUR)
+        got, st = s.ils(r, kicks, 5, kind)
+    assert st["final_length"] == wst["best_length"]
+    assert st["moves"] == wst["moves"] and st["accepted"] == wst["accepted"]
+    assert np.array_equal(got, want)
+
+
+def test_switching_back_to_the_exhaustive_search(lg, inst, oracle_mod):
+    xy, r = _case(lg, inst, "uniform", 2500, 31)
+    want, m, _ = oracle_mod.descend(xy, r, threads=THREADS)
+    with lg.Solver(xy) as s:
+        s.set_search(lg.SEARCH_NEIGHBOUR, 6)
+        s.optimize(r)
+        s.set_search(lg.SEARCH_EXHAUSTIVE)
+        got, st = s.optimize(r)
+        assert s.info()["descent_mode"] == lg.DESCENT_COOPERATIVE
+    assert np.array_equal(got, want) and st["moves"] == m
+    with lg.Solver(xy) as s, pytest.raises(lg.LogoError):
+        s.set_search(lg.SEARCH_NEIGHBOUR, 17)

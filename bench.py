@@ -334,6 +334,8 @@ def run_ours(a, world, rank, local, dist):
 
     # e2e: the C-ABI call with host buffers, one move per call
     cur = s.get_route()
+    info_route_io = {lg.ROUTE_IO_COPY: "copy", lg.ROUTE_IO_DIRECT: "direct"}.get(
+        s.info()["route_io"], "?")
     for _ in range(3):
         s.optimize_inplace(cur, max_moves=1)
     barrier(dist)
@@ -343,8 +345,10 @@ def run_ours(a, world, rank, local, dist):
     e2e_s = reduce_max(dist, time.perf_counter() - t0)
     e2e = {"value": world * pairs * a.e2e_steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n + 2 * 128,
-           "call": "logo_descend(max_moves=1) per step: route H2D, sweep, argmin, "
-                   "reversal, route D2H"}
+           "call": "logo_descend(max_moves=1) per step on the caller's host buffer: "
+                   "route in, sweep, argmin, reversal, route out (read and written in "
+                   "place by the device where it reaches pageable host memory, else "
+                   "copied)", "route_io": info_route_io}
 
     # roofline of the sweep (the dominant kernel: the boxed screen's three
     # launches, timed together by the events around logo_enqueue_sweep)

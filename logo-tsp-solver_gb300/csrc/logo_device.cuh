@@ -144,6 +144,21 @@ __host__ __device__ __forceinline__ uint32_t bridge_src(uint32_t k, uint32_t p1,
     return k;
 }
 
+// ---- programmatic dependent launch -------------------------------------------
+// Kernels of the step chain (route load, sweeps, move, route store) are
+// launched with programmatic stream serialization (launch_chained in
+// logo_internal.h): a kernel may be scheduled while the previous one drains.
+// Each calls chain_wait() before touching memory -- it returns once the
+// previous kernel has completed and its writes are visible, and is a no-op
+// for an ordinary launch -- and chain_release() right after, which lets the
+// next kernel of the chain be scheduled.  Because every CTA waits before it
+// can finish, a kernel completes only after its predecessor did, so the
+// chain stays ordered end to end.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---- warp / block reductions ----------------------------------------------
 __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
 #pragma unroll

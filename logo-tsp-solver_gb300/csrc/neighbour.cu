@@ -63,6 +63,8 @@ __global__ void __launch_bounds__(kNbrThreads)
                      const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
                      const uint32_t* __restrict__ pos, const uint32_t* __restrict__ nbr,
                      uint32_t K, uint32_t n, DevState* st) {
+    chain_wait();
+    chain_release();
     __shared__ unsigned long long red[kNbrThreads / 32];
     if (*(volatile unsigned int*)&st->converged) return;  // the same in every thread
     const bool cur = *(volatile unsigned int*)&st->cur;
@@ -117,9 +119,8 @@ __global__ void fill_pos_kernel(const uint32_t* __restrict__ R0, const uint32_t*
 cudaError_t launch_nbr_sweep(const NbrLaunch& L, cudaStream_t s) {
     const uint64_t blocks = ((uint64_t)L.n + kNbrThreads - 1) / kNbrThreads;
     const unsigned grid = (unsigned)(blocks < 1 ? 1 : (blocks > 8192 ? 8192 : blocks));
-    nbr_sweep_kernel<<<grid, kNbrThreads, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.nbr, L.K,
-                                                  L.n, L.st);
-    return cudaGetLastError();
+    return launch_chained(nbr_sweep_kernel, grid, kNbrThreads, 0, s, L.Q0, L.Q1, L.R0, L.R1,
+                          L.pos, L.nbr, L.K, L.n, L.st);
 }
 
 cudaError_t launch_fill_pos(const NbrLaunch& L, cudaStream_t s) {

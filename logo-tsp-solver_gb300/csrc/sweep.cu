@@ -42,6 +42,8 @@ __global__ void __launch_bounds__(NW * 32)
                  const OrderedCity* __restrict__ Q1, uint32_t n,
                  const uint2* __restrict__ tiles, uint32_t cb, float margin,
                  DevState* st) {
+    chain_wait();
+    chain_release();
     extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     uint64_t* wbest = reinterpret_cast<uint64_t*>(smem_raw + 8);  // NW <= 8
@@ -112,6 +114,8 @@ __global__ void __launch_bounds__(NW * 32)
     sweep_kernel5(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                   uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, float margin,
                   DevState* st) {
+    chain_wait();
+    chain_release();
     extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
@@ -190,6 +194,8 @@ __global__ void __launch_bounds__(NW * 32)
     sweep_kernel6(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                   uint32_t n, const uint2* __restrict__ tiles, uint32_t cb, float margin,
                   DevState* st) {
+    chain_wait();
+    chain_release();
     extern __shared__ __align__(32) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     OrderedCity* stage = reinterpret_cast<OrderedCity*>(smem_raw + 96);
@@ -344,6 +350,8 @@ __global__ void __launch_bounds__(256)
                        uint32_t n, float4* __restrict__ wbox, float* __restrict__ wmax,
                        float4* __restrict__ rbox, float* __restrict__ rmax,
                        uint32_t* __restrict__ workctl, DevState* st) {
+    chain_wait();
+    chain_release();
     if (*(volatile unsigned int*)&st->converged) return;
     if (blockIdx.x == 0 && threadIdx.x < 3) workctl[threadIdx.x] = 0u;
     const bool cur = *(volatile unsigned int*)&st->cur;
@@ -423,6 +431,8 @@ __global__ void __launch_bounds__(256)
                        const float4* __restrict__ rbox, const float* __restrict__ rmax,
                        uint4* __restrict__ work, uint32_t cap, uint32_t* __restrict__ workctl,
                        DevState* st) {
+    chain_wait();
+    chain_release();
     __shared__ float4 srb[kMaxTileRows / kWin6];
     __shared__ float sre[kMaxTileRows / kWin6];
     if (*(volatile unsigned int*)&st->converged) return;
@@ -565,6 +575,8 @@ __global__ void __launch_bounds__(NW * 32, boxed_min_blocks(R, NW))
                        const float* __restrict__ gmax, const uint4* __restrict__ work,
                        uint32_t cap, float margin, uint32_t* __restrict__ workctl,
                        DevState* st) {
+    chain_wait();
+    chain_release();
     static_assert(R <= 16 && NW * 32 <= 256, "unit encoding: 8-bit thread, 16-bit rows");
     constexpr int G = (128 / R) < 32 ? (128 / R) : 32;
     extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -738,9 +750,8 @@ static cudaError_t launch_sweep5_g(const SweepLaunch& L, cudaStream_t s, bool pr
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     attr_bytes(sweep5_smem_bytes(kMaxTileCols)));
     }
-    sweep_kernel5<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
-                                                           L.margin, L.st);
-    return cudaGetLastError();
+    return launch_chained(sweep_kernel5<R, NW, G>, L.ntiles, NW * 32, smem, s, L.Q0, L.Q1, L.n,
+                          L.tiles, L.cb, L.margin, L.st);
 }
 
 // Column grouping of the fused screen: on large tours few columns pass and
@@ -769,9 +780,8 @@ static cudaError_t launch_sweep6_g(const SweepLaunch& L, cudaStream_t s, bool pr
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     attr_bytes(sweep6_smem_bytes(kMaxTileCols)));
     }
-    sweep_kernel6<R, NW, G><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles, L.cb,
-                                                           L.margin, L.st);
-    return cudaGetLastError();
+    return launch_chained(sweep_kernel6<R, NW, G>, L.ntiles, NW * 32, smem, s, L.Q0, L.Q1, L.n,
+                          L.tiles, L.cb, L.margin, L.st);
 }
 
 // Boxed variant: window statistics with the near-neighbour seed, tile
@@ -803,21 +813,20 @@ static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool pre
     }
     const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
     const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
-    window_seed_kernel<<<(nwin + 7) / 8, 256, 0, s>>>(L.Q0, L.Q1, L.R0, L.R1, L.pos, L.nbr, L.n,
-                                                      L.wbox, L.wmax, L.rbox, L.rmax,
-                                                      L.workctl, L.st);
+    e = launch_chained(window_seed_kernel, (nwin + 7) / 8, 256, 0, s, L.Q0, L.Q1, L.R0, L.R1,
+                       L.pos, L.nbr, L.n, L.wbox, L.wmax, L.rbox, L.rmax, L.workctl, L.st);
+    if (e != cudaSuccess) return e;
     const uint32_t rows_per_tile = (uint32_t)(NW * 32 * R);
     const uint32_t row_blocks = (L.n - 4) / rows_per_tile + 1;  // row0 + 3 <= n
     // CTAs per row block: filter_steps(n) steps per warp for the longest row (block 0)
     const uint32_t steps = ((L.n - 3 + L.cb - 1) / L.cb + 32 / (L.cb / 32) - 1) / (32 / (L.cb / 32));
     const uint32_t fs = filter_steps(L.n);
     const dim3 fgrid(row_blocks, (steps + 8 * fs - 1) / (8 * fs));
-    tile_filter_kernel<<<fgrid, 256, 0, s>>>(L.n, rows_per_tile, L.cb, L.wbox, L.wmax, L.rbox,
-                                             L.rmax, L.work, L.ntiles, L.workctl, L.st);
-    sweep_boxed_kernel<R, NW><<<grid, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.cb, L.wbox, L.wmax,
-                                                          L.work, L.ntiles, L.margin, L.workctl,
-                                                          L.st);
-    return cudaGetLastError();
+    e = launch_chained(tile_filter_kernel, fgrid, 256, 0, s, L.n, rows_per_tile, L.cb, L.wbox,
+                       L.wmax, L.rbox, L.rmax, L.work, L.ntiles, L.workctl, L.st);
+    if (e != cudaSuccess) return e;
+    return launch_chained(sweep_boxed_kernel<R, NW>, grid, NW * 32, smem, s, L.Q0, L.Q1, L.n,
+                          L.cb, L.wbox, L.wmax, L.work, L.ntiles, L.margin, L.workctl, L.st);
 }
 
 // Column groups of the local-coordinate screen: 128 / R columns per branch
@@ -843,9 +852,8 @@ static cudaError_t launch_sweep_t(const SweepLaunch& L, cudaStream_t s, bool pre
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     attr_bytes(sweep_smem_bytes(kMaxTileCols)));
     }
-    sweep_kernel<R, NW><<<L.ntiles, NW * 32, smem, s>>>(L.Q0, L.Q1, L.n, L.tiles,
-                                                        L.cb, L.margin, L.st);
-    return cudaGetLastError();
+    return launch_chained(sweep_kernel<R, NW>, L.ntiles, NW * 32, smem, s, L.Q0, L.Q1, L.n,
+                          L.tiles, L.cb, L.margin, L.st);
 }
 
 static cudaError_t dispatch_sweep(const SweepLaunch& L, cudaStream_t s, bool prepare) {

@@ -15,10 +15,20 @@
 //   kick_kernel            ≙ ILSGlobalSolver::kick, ILSGlobalSolver.cpp:37-48
 //                            (and the double bridge, which has no reference)
 //   accept_kernel          ≙ accept/revert, ILSGlobalSolverSequential.cpp:87-94
+#include <cstdlib>
+
 #include "logo_device.cuh"
 #include "logo_internal.h"
 
 namespace logo {
+
+bool chained_launch_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("LOGO_CHAINED_LAUNCH");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 
 namespace {
 
@@ -30,12 +40,15 @@ inline unsigned grid_for(uint32_t n) {
 }
 
 // Last-CTA election: true in exactly one thread of the grid, after every
-// CTA has finished its writes.
+// CTA has finished its writes.  The CTA barrier orders its threads' writes
+// before thread 0's fence, which then makes them visible device-wide before
+// the counter moves (one fence per CTA, not one per thread: measured on
+// GB300 the per-thread fences were a tenth of the gather's stalls).
 __device__ __forceinline__ bool last_block_done(unsigned int* counter) {
     __shared__ bool last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+        __threadfence();
         unsigned prev = atomicAdd(counter, 1u);
         last = (prev == gridDim.x - 1);
     }
@@ -63,6 +76,8 @@ __global__ void load_route_kernel(const float2* __restrict__ xy, const uint32_t*
                                   uint32_t* __restrict__ seen, uint32_t epoch,
                                   uint32_t* __restrict__ pos, DevState* st,
                                   unsigned long long reset_moves) {
+    chain_wait();
+    chain_release();
     bool bad = false;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x) {
@@ -105,6 +120,8 @@ __global__ void store_route_kernel(const uint32_t* __restrict__ R0,
                                    const uint32_t* __restrict__ R1,
                                    const uint32_t* __restrict__ Rbest, uint32_t* dst,
                                    uint32_t n, const DevState* st, int best) {
+    chain_wait();
+    chain_release();
     const uint32_t* R = best ? Rbest : (*(volatile const unsigned int*)&st->cur ? R1 : R0);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x)
@@ -112,6 +129,8 @@ __global__ void store_route_kernel(const uint32_t* __restrict__ R0,
 }
 
 __global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves) {
+    chain_wait();
+    chain_release();
     st->best_key = kNoMove;
     st->moves = 0;
     st->nbr_sweeps = 0;
@@ -149,6 +168,8 @@ __device__ __forceinline__ void gather_tour(const OrderedCity* __restrict__ Qs,
 }
 
 __global__ void apply_move_kernel(TourBufs T) {
+    chain_wait();
+    chain_release();
     DevState* st = T.st;
     if (*(volatile unsigned int*)&st->converged) return;
     const uint64_t key = *(volatile unsigned long long*)&st->best_key;
@@ -343,25 +364,22 @@ cudaError_t launch_kick_cond(DevState* st, cudaGraphConditionalHandle h, bool fi
 
 cudaError_t launch_load_route(const TourBufs& T, const uint32_t* src, uint32_t epoch,
                               unsigned long long reset_moves, cudaStream_t s) {
-    load_route_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.xy, src, T.route[0], T.Q[0], T.n,
-                                                         T.seen, epoch, T.pos, T.st,
-                                                         reset_moves);
-    return cudaGetLastError();
+    return launch_chained(load_route_kernel, grid_for(T.n), kThreads, 0, s, T.xy, src,
+                          T.route[0], T.Q[0], T.n, T.seen, epoch, T.pos, T.st, reset_moves);
 }
 
 cudaError_t launch_store_route(const TourBufs& T, uint32_t* dst, bool best, cudaStream_t s) {
-    store_route_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T.route[0], T.route[1],
-                                                          T.route_best, dst, T.n, T.st,
-                                                          best ? 1 : 0);
-    return cudaGetLastError();
+    return launch_chained(store_route_kernel, grid_for(T.n), kThreads, 0, s, T.route[0],
+                          T.route[1], T.route_best, dst, T.n, T.st, best ? 1 : 0);
 }
 
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,
                                  cudaStream_t s) {
-    reset_descent_kernel<<<1, 1, 0, s>>>(T.st, max_moves);
-    return cudaGetLastError();
+    return launch_chained(reset_descent_kernel, 1, 1, 0, s, T.st, max_moves);
 }
 __global__ void resume_descent_kernel(DevState* st) {
+    chain_wait();
+    chain_release();
     const unsigned int bad = st->status | st->bad_route;  // includes the move limit
     if (!bad) {
         st->converged = 0u;
@@ -370,13 +388,11 @@ __global__ void resume_descent_kernel(DevState* st) {
 }
 
 cudaError_t launch_resume_descent(const TourBufs& T, cudaStream_t s) {
-    resume_descent_kernel<<<1, 1, 0, s>>>(T.st);
-    return cudaGetLastError();
+    return launch_chained(resume_descent_kernel, 1, 1, 0, s, T.st);
 }
 
 cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s) {
-    apply_move_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);
-    return cudaGetLastError();
+    return launch_chained(apply_move_kernel, grid_for(T.n), kThreads, 0, s, T);
 }
 cudaError_t launch_tour_length(const TourBufs& T, cudaStream_t s) {
     tour_length_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);

@@ -530,6 +530,8 @@ def run_large(a, device):
     # the same call with the neighbour-list search (8 nearest cities, then
     # full sweeps): another path to 2-opt local optima, not the reference's
     out["neighbour_search"] = one(lg.SEARCH_NEIGHBOUR, 8)
+    # and with Or-opt moves among the neighbour candidates
+    out["neighbour_oropt_search"] = one(lg.SEARCH_NEIGHBOUR_OROPT, 8)
     return out
 
 

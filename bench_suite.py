@@ -185,6 +185,29 @@ def cmd_construct(a):
                       "end_to_end_device_mf_s": mf_dev_s, "identical_results_mf": same_mf}))
 
 
+def cmd_search(a):
+    """Descent of bench.py's instance (n = --n, Gaussian mixture, NN start)
+    with the neighbour-list search (--k nearest cities), limited to --limit
+    moves (0: to the local optimum), beside the exhaustive search."""
+    import bench
+    xy, r0 = bench.workload(a.n, a.seed)
+    res = []
+    for search, k in ((lg.SEARCH_NEIGHBOUR, a.k), (lg.SEARCH_EXHAUSTIVE, 0)):
+        if search == lg.SEARCH_EXHAUSTIVE and a.limit:
+            continue  # profiling runs: the neighbour search alone
+        with lg.Solver(xy) as s:
+            s.set_search(search, k)
+            t0 = time.perf_counter()
+            got, st = s.optimize(r0, max_moves=a.limit)
+            wall = time.perf_counter() - t0
+        res.append({"search": "neighbour" if search else "exhaustive", "k": k,
+                    "wall_s": wall, "moves": st["moves"], "sweeps": st["sweeps"],
+                    "final_length": st["final_length"], "pair_evals": st["pair_evals"]})
+    print(json.dumps({"workload": f"n={a.n} Gaussian mixture, NN start, descent"
+                                  + (f" limited to {a.limit} moves" if a.limit else ""),
+                      "results": res}))
+
+
 def _pool(count, seed, n_lo, n_hi):
     """Serving instances: n log-uniform in [n_lo, n_hi], clustered or uniform
     (50/50 by seed) in [0,1e6)^2, nearest-neighbour start tours."""
@@ -332,7 +355,10 @@ def cmd_serve(a):
 
 def main():
     p = argparse.ArgumentParser()
-    p.add_argument("cmd", choices=["plain", "sweep", "large", "serve", "construct"])
+    p.add_argument("cmd", choices=["plain", "sweep", "large", "serve", "construct", "search"])
+    p.add_argument("--n", type=int, default=100000, help="search: cities")
+    p.add_argument("--k", type=int, default=8, help="search: neighbour-list length")
+    p.add_argument("--limit", type=int, default=0, help="search: move limit (0: none)")
     p.add_argument("--seeds", type=int, default=4)
     p.add_argument("--count", type=int, default=4096, help="construct: instances")
     p.add_argument("--seed", type=int, default=2)
@@ -356,7 +382,7 @@ def main():
         a.kicks = {"large": 1000, "serve": 50}.get(a.cmd, 0)
     lg.load()
     {"plain": cmd_plain, "sweep": cmd_sweep, "large": cmd_large, "serve": cmd_serve,
-     "construct": cmd_construct}[a.cmd](a)
+     "construct": cmd_construct, "search": cmd_search}[a.cmd](a)
 
 
 if __name__ == "__main__":

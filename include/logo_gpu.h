@@ -506,10 +506,17 @@ logo_status logo_ctx_set_route_io(logo_ctx *ctx, int mode);
  *   along another path than the reference's, in far fewer pair evaluations
  *   at large n (no counterpart in the reference).  Descents in this mode
  *   always use graph launches (not the cooperative kernel).
+ * LOGO_SEARCH_NEIGHBOUR_OROPT: as NEIGHBOUR, and each step also weighs the
+ *   Or-opt moves that create an edge to a listed neighbour: a segment of 1
+ *   to 3 cities moved, in order or reversed, into another gap of the tour
+ *   (neither side of the closing edge is cut); the lowest delta wins, ties
+ *   to the 2-opt move, then to shorter and unreversed segments, then to the
+ *   lower (segment start, gap).
  * neighbours: 1..16, 0 = 8.  INVALID_ARG for an unknown mode or list
  * length. */
 #define LOGO_SEARCH_EXHAUSTIVE 0
 #define LOGO_SEARCH_NEIGHBOUR 1
+#define LOGO_SEARCH_NEIGHBOUR_OROPT 2
 logo_status logo_ctx_set_search(logo_ctx *ctx, int mode, uint32_t neighbours);
 
 /* Sweep kernel variants; all return identical moves (the default depends on

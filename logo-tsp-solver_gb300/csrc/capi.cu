@@ -122,7 +122,16 @@ NbrLaunch nbr_args(const logo_ctx* c) {
     L.K = c->search_k;
     L.n = c->n;
     L.st = c->d_st;
+    L.oropt = c->search == LOGO_SEARCH_NEIGHBOUR_OROPT;
+    L.margin = c->margin;
     return L;
+}
+
+// The move step after a neighbour sweep: with Or-opt candidates the apply
+// kernel that also reads their slots.
+cudaError_t launch_nbr_apply(const logo_ctx* c, const TourBufs& T, cudaStream_t s) {
+    return c->search == LOGO_SEARCH_NEIGHBOUR_OROPT ? launch_apply_nbr_move(T, s)
+                                                    : launch_apply_move(T, s);
 }
 
 SweepLaunch sweep_args(const logo_ctx* c) {
@@ -154,10 +163,12 @@ SweepLaunch sweep_args(const logo_ctx* c) {
 uint64_t pairs_of(uint32_t n) { return n < 4 ? 0 : (uint64_t)(n - 2) * (n - 3) / 2; }
 
 // Pairs decided by `sweeps` sweeps of which `nbr` were neighbour sweeps
-// (2K candidate pairs per position).
+// (2K candidate 2-opt pairs per position, and 10K Or-opt candidates with
+// LOGO_SEARCH_NEIGHBOUR_OROPT).
 uint64_t pair_evals_of(const logo_ctx* c, uint64_t sweeps, uint64_t nbr) {
     nbr = std::min(nbr, sweeps);
-    return (sweeps - nbr) * pairs_of(c->n) + nbr * 2ull * c->search_k * c->n;
+    const uint64_t per = (c->search == LOGO_SEARCH_NEIGHBOUR_OROPT ? 12ull : 2ull) * c->search_k;
+    return (sweeps - nbr) * pairs_of(c->n) + nbr * per * c->n;
 }
 
 // Default tile shape by size (overridable through logo_ctx_set_shape and
@@ -291,14 +302,14 @@ logo_status rebuild(logo_ctx* c) {
     e = cudaGraphInstantiate(&c->chunk_exec, g, 0);
     cudaGraphDestroy(g);
     CK(c, e);
-    if (c->search == LOGO_SEARCH_NEIGHBOUR) {
+    if (c->search != LOGO_SEARCH_EXHAUSTIVE) {
         g = nullptr;
         CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         const NbrLaunch N = nbr_args(c);
         e = cudaSuccess;
         for (uint32_t s = 0; s < c->nbr_chunk_steps && e == cudaSuccess; ++s) {
             e = launch_nbr_sweep(N, c->stream);
-            if (e == cudaSuccess) e = launch_apply_move(T, c->stream);
+            if (e == cudaSuccess) e = launch_nbr_apply(c, T, c->stream);
         }
         e2 = cudaStreamEndCapture(c->stream, &g);
         if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -407,7 +418,7 @@ cudaError_t capture_sweep_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
         cudaError_t eb = cudaSuccess;
         for (uint32_t k = 0; k < steps && eb == cudaSuccess; ++k) {
             eb = nbr ? launch_nbr_sweep(N, b) : launch_sweep(L, b);
-            if (eb == cudaSuccess) eb = launch_apply_move(T, b);
+            if (eb == cudaSuccess) eb = nbr ? launch_nbr_apply(c, T, b) : launch_apply_move(T, b);
         }
         if (eb == cudaSuccess) eb = launch_descent_cond(st, h, false, b);
         return eb;
@@ -418,7 +429,7 @@ cudaError_t capture_sweep_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
 // LOGO_SEARCH_NEIGHBOUR the neighbour loop, a resume and the full loop.
 cudaError_t capture_descent_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
                                  cudaStream_t bs) {
-    if (c->search != LOGO_SEARCH_NEIGHBOUR) return capture_sweep_loop(c, s, g, bs, false);
+    if (c->search == LOGO_SEARCH_EXHAUSTIVE) return capture_sweep_loop(c, s, g, bs, false);
     cudaError_t e = capture_sweep_loop(c, s, g, bs, true);
     if (e == cudaSuccess) e = launch_resume_descent(bufs(c), s);
     if (e == cudaSuccess) e = capture_sweep_loop(c, s, g, bs, false);
@@ -619,7 +630,7 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
         if (s != LOGO_OK) return s;
         if (!c->h_st->converged && !c->h_st->status)
             return fail(c, LOGO_ERR_DEVICE_FAULT, "cooperative descent did not finish");
-    } else if (c->search == LOGO_SEARCH_NEIGHBOUR) {
+    } else if (c->search != LOGO_SEARCH_EXHAUSTIVE) {
         // neighbour sweeps until no candidate improves, then full sweeps
         logo_status s = graph_descent(c, max_moves, reset, moves0, moves0, nullptr, nullptr,
                                       true);
@@ -660,7 +671,7 @@ logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool partial_ok, uint
             const TourBufs T = bufs(c);
             for (uint64_t k = 0; k < left; ++k) {
                 CK(c, nbr ? launch_nbr_sweep(N, c->stream) : launch_sweep(L, c->stream));
-                CK(c, launch_apply_move(T, c->stream));
+                CK(c, nbr ? launch_nbr_apply(c, T, c->stream) : launch_apply_move(T, c->stream));
             }
             if (route_out) {
                 logo_status s = enqueue_route_out(c, route_out, false);
@@ -918,7 +929,8 @@ logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
 logo_status logo_ctx_set_search(logo_ctx* c, int mode, uint32_t neighbours) {
     if (!c) return LOGO_ERR_INVALID_ARG;
     if (c->poisoned) return poisoned_error(c);
-    if (mode != LOGO_SEARCH_EXHAUSTIVE && mode != LOGO_SEARCH_NEIGHBOUR)
+    if (mode != LOGO_SEARCH_EXHAUSTIVE && mode != LOGO_SEARCH_NEIGHBOUR &&
+        mode != LOGO_SEARCH_NEIGHBOUR_OROPT)
         return fail(c, LOGO_ERR_INVALID_ARG, "unknown search mode");
     if (neighbours == 0) neighbours = kSearchNeighbours;
     if (neighbours > kSearchNeighboursMax)
@@ -929,7 +941,7 @@ logo_status logo_ctx_set_search(logo_ctx* c, int mode, uint32_t neighbours) {
     CK(c, cudaStreamSynchronize(c->stream));
     c->search = mode;
     c->search_k = neighbours;
-    if (mode == LOGO_SEARCH_NEIGHBOUR) {
+    if (mode != LOGO_SEARCH_EXHAUSTIVE) {
         logo_status s = prepare_search(c);
         if (s != LOGO_OK) return s;
     }

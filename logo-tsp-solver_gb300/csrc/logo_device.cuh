@@ -69,6 +69,7 @@ struct DevState {
     unsigned int kick_kind;         // LOGO_KICK_SEGMENT or LOGO_KICK_DOUBLE_BRIDGE
     unsigned int load_bad;          // set by a CTA of load_route_kernel that met a bad id
     unsigned long long nbr_sweeps;  // neighbour sweeps of this descent (or ILS call)
+    unsigned long long or_key[5];   // best Or-opt candidate per variant (see or_slot)
 };
 
 __host__ __device__ __forceinline__ uint64_t pack_key(int delta, uint32_t i,
@@ -142,6 +143,37 @@ __host__ __device__ __forceinline__ uint32_t bridge_src(uint32_t k, uint32_t p1,
     if (k < p1 + l2) return p2 + (k - p1);
     if (k < p3) return p1 + (k - p1 - l2);
     return k;
+}
+
+// ---- Or-opt moves of the neighbour search -------------------------------------
+// Segment [s, s+L) (L = 1..3, 1 <= s, s+L <= n-1) moved into the gap after
+// old position p (p + 1 <= s - 1, or s + L <= p <= n - 2), in tour order
+// (forward) or reversed.  Variants in tie order: slot 0 = L1, 1 = L2, 2 = L2
+// reversed, 3 = L3, 4 = L3 reversed; each slot keeps pack_key(delta, s, p).
+constexpr int kOrSlots = 5;
+__host__ __device__ __forceinline__ int or_slot(uint32_t L, bool rev) {
+    return L == 1 ? 0 : (int)(2 * L - 3) + (rev ? 1 : 0);
+}
+__host__ __device__ __forceinline__ uint32_t or_len(int slot) {
+    return slot == 0 ? 1u : (uint32_t)((slot + 3) / 2);
+}
+__host__ __device__ __forceinline__ bool or_rev(int slot) { return slot == 2 || slot == 4; }
+// Source position of new position k after the Or-opt move (s, L, p, rev).
+__host__ __device__ __forceinline__ uint32_t oropt_src(uint32_t k, uint32_t s, uint32_t L,
+                                                       uint32_t p, bool rev) {
+    if (p >= s + L) {  // the segment moves right: old[0,s) old[s+L,p] seg old[p+1,n)
+        if (k < s || k > p) return k;
+        if (k < p + 1 - L) return k + L;
+        const uint32_t t = k - (p + 1 - L);
+        return rev ? s + L - 1 - t : s + t;
+    }
+    // the segment moves left: old[0,p] seg old[p+1,s) old[s+L,n)
+    if (k <= p || k >= s + L) return k;
+    if (k < p + 1 + L) {
+        const uint32_t t = k - (p + 1);
+        return rev ? s + L - 1 - t : s + t;
+    }
+    return k - L;
 }
 
 // ---- programmatic dependent launch -------------------------------------------

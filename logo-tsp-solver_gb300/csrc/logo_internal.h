@@ -100,6 +100,8 @@ struct NbrLaunch {
     uint32_t K;
     uint32_t n;
     DevState* st;
+    bool oropt;           // also the Or-opt candidates (into st->or_key)
+    float margin;         // filter_margin of the instance (Or-opt estimate test)
 };
 // Default and largest neighbour-list length of LOGO_SEARCH_NEIGHBOUR.
 constexpr uint32_t kSearchNeighbours = 8, kSearchNeighboursMax = 16;
@@ -176,6 +178,9 @@ cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves
                                  cudaStream_t s);
 // Applies the move in st->best_key (or marks convergence).
 cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s);
+// The same for the neighbour search with Or-opt moves: the best of
+// st->best_key and st->or_key[].
+cudaError_t launch_apply_nbr_move(const TourBufs& T, cudaStream_t s);
 // After a converged neighbour phase: continue the same descent (moves and
 // limit kept) with full sweeps, unless it stopped on an error or the limit.
 cudaError_t launch_resume_descent(const TourBufs& T, cudaStream_t s);

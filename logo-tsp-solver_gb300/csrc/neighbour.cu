@@ -16,6 +16,8 @@
 // another path (no counterpart in the reference; the classic neighbour-list
 // restriction of 2-opt, with the candidate order fixed by the packed key).
 #include <algorithm>
+#include <atomic>
+#include <climits>
 
 #include "logo_device.cuh"
 #include "logo_internal.h"
@@ -24,7 +26,7 @@ namespace logo {
 
 namespace {
 
-constexpr int kNbrThreads = 256;
+constexpr int kNbrThreads = 256, kNbrThreadsOr = 128;
 constexpr uint32_t kNbrBatch = 4;  // neighbours whose loads are issued together
 
 // The two candidate pairs of position i (qim, qi, qip: positions i-1, i,
@@ -55,26 +57,86 @@ __device__ __forceinline__ void nbr_pairs(uint32_t i, uint32_t p, uint32_t n, Or
     }
 }
 
-// One thread per tour position; its neighbours in batches of kNbrBatch,
-// every load of a batch issued before any is used (indices clamped into
-// range, so the loads of pairs that do not exist are harmless).
-__global__ void __launch_bounds__(kNbrThreads)
+// An Or-opt candidate of the segment [s, s+L) (first and last: its end
+// cities) moved into the gap after old position p (qp, qp1: positions p and
+// p+1); base = d(s-1, s+L) - e[s] - e[s+L], or INT_MAX where the segment
+// does not exist.  Forward: new edges (p, s) and (s+L-1, p+1); reversed:
+// (p, s+L-1) and (s, p+1).  The two new distances are first estimated with
+// the MUFU square root: the exact delta is at least the estimate minus M
+// (filter_margin: two approximate distances, three roundings of magnitudes
+// up to four diagonals, as for a 2-opt pair), so an estimate >= M rules the
+// candidate out and only the others are evaluated exactly.
+template <int L, bool REV>
+__device__ __forceinline__ void or_try(uint32_t s, uint32_t p, uint32_t n,
+                                       const OrderedCity& first, const OrderedCity& last,
+                                       int base, float M, const OrderedCity& qp,
+                                       const OrderedCity& qp1, uint64_t* bo) {
+    if (base == INT_MAX) return;
+    if (!(p + 2 <= s || (p >= s + (uint32_t)L && p + 2 <= n))) return;
+    const OrderedCity& u = REV ? last : first;
+    const OrderedCity& w = REV ? first : last;
+    const float v = (float)base + approx_dist(qp.x, qp.y, u.x, u.y) +
+                    (approx_dist(w.x, w.y, qp1.x, qp1.y) - qp1.e);
+    if (!(v < M)) return;
+    const int delta = base + exact_dist(qp.x, qp.y, u.x, u.y) +
+                      exact_dist(w.x, w.y, qp1.x, qp1.y) - (int)qp1.e;
+    if (delta < 0) {
+        constexpr int slot = L == 1 ? 0 : 2 * L - 3 + (REV ? 1 : 0);
+        const uint64_t key = pack_key(delta, s, p);
+        bo[slot] = key < bo[slot] ? key : bo[slot];
+    }
+}
+
+// One thread per tour position i; its city's neighbours in batches of
+// kNbrBatch, every load of a batch issued before any is used (indices
+// clamped into range, so the loads of candidates that do not exist are
+// harmless).  With OR the same loads also serve the Or-opt candidates in
+// which the city at i is a segment end: as the first city of the segments
+// starting at i (lengths 1-3) and as the last city of the segments [i-1, i+1)
+// and [i-2, i+1) -- every Or-opt candidate of the neighbour search exactly
+// once per list entry, the same set as walking each segment's two end lists.
+template <bool OR, int NT>
+__global__ void __launch_bounds__(NT)
     nbr_sweep_kernel(const OrderedCity* __restrict__ Q0, const OrderedCity* __restrict__ Q1,
                      const uint32_t* __restrict__ R0, const uint32_t* __restrict__ R1,
                      const uint32_t* __restrict__ pos, const uint32_t* __restrict__ nbr,
-                     uint32_t K, uint32_t n, DevState* st) {
+                     uint32_t K, uint32_t n, float M, DevState* st) {
     chain_wait();
     chain_release();
-    __shared__ unsigned long long red[kNbrThreads / 32];
+    __shared__ unsigned long long red[NT / 32];
+    __shared__ unsigned long long red_or[OR ? kOrSlots : 1][NT / 32];
     if (*(volatile unsigned int*)&st->converged) return;  // the same in every thread
     const bool cur = *(volatile unsigned int*)&st->cur;
     const OrderedCity* Q = cur ? Q1 : Q0;
     const uint32_t* R = cur ? R1 : R0;
     uint64_t best = kNoMove;
+    uint64_t bo[kOrSlots];
+#pragma unroll
+    for (int v = 0; v < kOrSlots; ++v) bo[v] = kNoMove;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += gridDim.x * blockDim.x) {
         const uint32_t city = min(R[i], n - 1);
         const OrderedCity qim = Q[i >= 1 ? i - 1 : 0], qi = Q[i], qip = Q[min(i + 1, n - 1)];
+        // Or-opt: positions i-3 .. i+3 and the bases d(s-1, s+L) - e[s] - e[s+L]
+        // of the segments (s, L) = (i, 1), (i, 2), (i, 3), (i-1, 2), (i-2, 3)
+        OrderedCity qm3, qm2, qp2, qp3;
+        int b1 = INT_MAX, b2 = INT_MAX, b3 = INT_MAX, c2 = INT_MAX, c3 = INT_MAX;
+        if (OR) {
+            qm3 = Q[i >= 3 ? i - 3 : 0];
+            qm2 = Q[i >= 2 ? i - 2 : 0];
+            qp2 = Q[min(i + 2, n - 1)];
+            qp3 = Q[min(i + 3, n - 1)];
+            if (i >= 1 && i + 1 <= n - 1)
+                b1 = exact_dist(qim.x, qim.y, qip.x, qip.y) - (int)qi.e - (int)qip.e;
+            if (i >= 1 && i + 2 <= n - 1)
+                b2 = exact_dist(qim.x, qim.y, qp2.x, qp2.y) - (int)qi.e - (int)qp2.e;
+            if (i >= 1 && i + 3 <= n - 1)
+                b3 = exact_dist(qim.x, qim.y, qp3.x, qp3.y) - (int)qi.e - (int)qp3.e;
+            if (i >= 2 && i + 1 <= n - 1)  // segment [i-1, i+1): s-1 = i-2, s+L = i+1
+                c2 = exact_dist(qm2.x, qm2.y, qip.x, qip.y) - (int)qim.e - (int)qip.e;
+            if (i >= 3 && i + 1 <= n - 1)  // segment [i-2, i+1): s-1 = i-3, s+L = i+1
+                c3 = exact_dist(qm3.x, qm3.y, qip.x, qip.y) - (int)qm2.e - (int)qip.e;
+        }
         const uint32_t* nb = nbr + (size_t)city * K;
         for (uint32_t k0 = 0; k0 < K; k0 += kNbrBatch) {
             uint32_t p[kNbrBatch];
@@ -90,18 +152,54 @@ __global__ void __launch_bounds__(kNbrThreads)
                 qpp[j] = Q[min(p[j] + 1, n - 1)];
             }
 #pragma unroll
-            for (uint32_t j = 0; j < kNbrBatch; ++j)
-                if (k0 + j < K) nbr_pairs(i, p[j], n, qim, qi, qip, qpm[j], qp[j], qpp[j], best);
+            for (uint32_t j = 0; j < kNbrBatch; ++j) {
+                if (k0 + j >= K) continue;
+                nbr_pairs(i, p[j], n, qim, qi, qip, qpm[j], qp[j], qpp[j], best);
+                if (!OR) continue;
+                const uint32_t q = p[j];
+                // the city at i first in the segments starting at i
+                or_try<1, false>(i, q, n, qi, qi, b1, M, qp[j], qpp[j], bo);
+                or_try<2, false>(i, q, n, qi, qip, b2, M, qp[j], qpp[j], bo);
+                or_try<3, false>(i, q, n, qi, qp2, b3, M, qp[j], qpp[j], bo);
+                if (q >= 1) {
+                    or_try<1, false>(i, q - 1, n, qi, qi, b1, M, qpm[j], qp[j], bo);
+                    or_try<2, true>(i, q - 1, n, qi, qip, b2, M, qpm[j], qp[j], bo);
+                    or_try<3, true>(i, q - 1, n, qi, qp2, b3, M, qpm[j], qp[j], bo);
+                }
+                // the city at i last in the segments [i-1, i+1) and [i-2, i+1)
+                if (i >= 2) {
+                    or_try<2, true>(i - 1, q, n, qim, qi, c2, M, qp[j], qpp[j], bo);
+                    if (q >= 1) or_try<2, false>(i - 1, q - 1, n, qim, qi, c2, M, qpm[j], qp[j], bo);
+                }
+                if (i >= 3) {
+                    or_try<3, true>(i - 2, q, n, qm2, qi, c3, M, qp[j], qpp[j], bo);
+                    if (q >= 1) or_try<3, false>(i - 2, q - 1, n, qm2, qi, c3, M, qpm[j], qp[j], bo);
+                }
+            }
         }
     }
     best = warp_min_u64(best);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) red[warp] = best;
+    if (OR) {
+#pragma unroll
+        for (int v = 0; v < kOrSlots; ++v) {
+            const uint64_t m = warp_min_u64(bo[v]);
+            if (lane == 0) red_or[v][warp] = m;
+        }
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         uint64_t m = red[0];
-        for (int w = 1; w < kNbrThreads / 32; ++w) m = red[w] < m ? red[w] : m;
+        for (int w = 1; w < NT / 32; ++w) m = red[w] < m ? red[w] : m;
         if (m != kNoMove) atomicMin(&st->best_key, (unsigned long long)m);
+        if (OR) {
+            for (int v = 0; v < kOrSlots; ++v) {
+                uint64_t mv = red_or[v][0];
+                for (int w = 1; w < NT / 32; ++w) mv = red_or[v][w] < mv ? red_or[v][w] : mv;
+                if (mv != kNoMove) atomicMin(&st->or_key[v], (unsigned long long)mv);
+            }
+        }
         if (blockIdx.x == 0) st->nbr_sweeps += 1;
     }
 }
@@ -117,10 +215,36 @@ __global__ void fill_pos_kernel(const uint32_t* __restrict__ R0, const uint32_t*
 }  // namespace
 
 cudaError_t launch_nbr_sweep(const NbrLaunch& L, cudaStream_t s) {
-    const uint64_t blocks = ((uint64_t)L.n + kNbrThreads - 1) / kNbrThreads;
-    const unsigned grid = (unsigned)(blocks < 1 ? 1 : (blocks > 8192 ? 8192 : blocks));
-    return launch_chained(nbr_sweep_kernel, grid, kNbrThreads, 0, s, L.Q0, L.Q1, L.R0, L.R1,
-                          L.pos, L.nbr, L.K, L.n, L.st);
+    // the Or-opt variant holds more state per thread: smaller CTAs keep one
+    // wave resident
+    const int nt = L.oropt ? kNbrThreadsOr : kNbrThreads;
+    const uint64_t blocks = ((uint64_t)L.n + nt - 1) / nt;
+    unsigned grid = (unsigned)(blocks < 1 ? 1 : (blocks > 16384 ? 16384 : blocks));
+    if (L.oropt) {
+        // no more CTAs than are resident at once (the loop strides over the
+        // rest): a second wave of a few CTAs would cost a whole CTA's time
+        static std::atomic<unsigned> resident[64];
+        int device = 0;
+        cudaError_t e = cudaGetDevice(&device);
+        if (e != cudaSuccess) return e;
+        unsigned r = resident[(unsigned)device % 64].load(std::memory_order_relaxed);
+        if (r == 0) {
+            int sms = 0, per_sm = 0;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, nbr_sweep_kernel<true, kNbrThreadsOr>, kNbrThreadsOr, 0);
+            if (e != cudaSuccess) return e;
+            r = (unsigned)(per_sm > 0 ? per_sm : 1) * (unsigned)sms;
+            resident[(unsigned)device % 64].store(r, std::memory_order_relaxed);
+        }
+        grid = grid < r ? grid : r;
+    }
+    if (L.oropt)
+        return launch_chained(nbr_sweep_kernel<true, kNbrThreadsOr>, grid, kNbrThreadsOr, 0, s,
+                              L.Q0, L.Q1, L.R0, L.R1, L.pos, L.nbr, L.K, L.n, L.margin, L.st);
+    return launch_chained(nbr_sweep_kernel<false, kNbrThreads>, grid, kNbrThreads, 0, s, L.Q0,
+                          L.Q1, L.R0, L.R1, L.pos, L.nbr, L.K, L.n, L.margin, L.st);
 }
 
 cudaError_t launch_fill_pos(const NbrLaunch& L, cudaStream_t s) {

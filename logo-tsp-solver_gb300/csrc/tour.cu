@@ -104,6 +104,7 @@ __global__ void load_route_kernel(const float2* __restrict__ xy, const uint32_t*
         st->cur = 0u;
         if (reset_moves) {
             st->best_key = kNoMove;
+            for (int v = 0; v < kOrSlots; ++v) st->or_key[v] = kNoMove;
             st->moves = 0;
             st->nbr_sweeps = 0;
             st->status = 0u;
@@ -132,6 +133,7 @@ __global__ void reset_descent_kernel(DevState* st, unsigned long long max_moves)
     chain_wait();
     chain_release();
     st->best_key = kNoMove;
+    for (int v = 0; v < kOrSlots; ++v) st->or_key[v] = kNoMove;
     st->moves = 0;
     st->nbr_sweeps = 0;
     st->status = 0u;
@@ -267,6 +269,7 @@ __global__ void kick_kernel(TourBufs T, int kind) {
         st->cur = cur ^ 1;
         st->kicks += 1;
         st->best_key = kNoMove;
+        for (int v = 0; v < kOrSlots; ++v) st->or_key[v] = kNoMove;
         st->moves = 0;
         st->converged = 0;
     }
@@ -377,6 +380,79 @@ cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves
                                  cudaStream_t s) {
     return launch_chained(reset_descent_kernel, 1, 1, 0, s, T.st, max_moves);
 }
+// The neighbour search with Or-opt moves: the lowest delta of the 2-opt
+// candidate (st->best_key) and the five Or-opt slots, ties to the 2-opt
+// move and then to the lower slot; applied as one gather (or marks
+// convergence).  Trace entries of Or-opt moves are (delta, -1 - (s + slot *
+// 2^21), p).
+__global__ void apply_nbr_move_kernel(TourBufs T) {
+    chain_wait();
+    chain_release();
+    DevState* st = T.st;
+    if (*(volatile unsigned int*)&st->converged) return;
+    const uint64_t key2 = *(volatile unsigned long long*)&st->best_key;
+    int slot = -1;
+    uint64_t key = key2;
+    for (int v = 0; v < kOrSlots; ++v) {
+        const uint64_t k = *(volatile unsigned long long*)&st->or_key[v];
+        if (k != kNoMove && (key == kNoMove || key_delta(k) < key_delta(key))) {
+            key = k;
+            slot = v;
+        }
+    }
+    const uint32_t cur = *(volatile unsigned int*)&st->cur;
+    const uint32_t n = T.n;
+    if (key == kNoMove) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->converged = 1;
+            st->sweeps += 1;
+        }
+        return;
+    }
+    const uint32_t a = key_i(key), b = key_j(key);
+    const uint32_t L = slot >= 0 ? or_len(slot) : 0u;
+    const bool rev = slot >= 0 && or_rev(slot);
+    const bool ok = slot < 0 ? (a >= 1 && b < n && b >= a + 2)
+                             : (a >= 1 && a + L <= n - 1 &&
+                                (b + 2 <= a || (b >= a + L && b + 2 <= n)));
+    if (!ok) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            atomicOr(&st->status, kErrBadKey);
+            st->converged = 1;
+        }
+        return;
+    }
+    OrderedCity* Qs = cur ? T.Q[1] : T.Q[0];
+    uint32_t* Rs = cur ? T.route[1] : T.route[0];
+    OrderedCity* Qd = cur ? T.Q[0] : T.Q[1];
+    uint32_t* Rd = cur ? T.route[0] : T.route[1];
+    if (slot < 0)
+        gather_tour(Qs, Rs, Qd, Rd, n, T.pos,
+                    [=] __device__(uint32_t k) { return rotrev_src(k, a, b, n); });
+    else
+        gather_tour(Qs, Rs, Qd, Rd, n, T.pos,
+                    [=] __device__(uint32_t k) { return oropt_src(k, a, L, b, rev); });
+    if (last_block_done(&st->done_blocks)) {
+        const unsigned long long m = st->moves;
+        if (st->move_log && m < st->log_cap) {
+            st->move_log[3 * m + 0] = key_delta(key);
+            st->move_log[3 * m + 1] =
+                slot < 0 ? (int)a : -1 - (int)(a + ((uint32_t)slot << 21));
+            st->move_log[3 * m + 2] = (int)b;
+        }
+        st->moves = m + 1;
+        st->total_moves += 1;
+        st->sweeps += 1;
+        st->best_key = kNoMove;
+        for (int v = 0; v < kOrSlots; ++v) st->or_key[v] = kNoMove;
+        st->cur = cur ^ 1;
+        if (m + 1 >= st->max_moves) {
+            st->converged = 1;
+            atomicOr(&st->status, kErrMoveLimit);
+        }
+    }
+}
+
 __global__ void resume_descent_kernel(DevState* st) {
     chain_wait();
     chain_release();
@@ -384,11 +460,16 @@ __global__ void resume_descent_kernel(DevState* st) {
     if (!bad) {
         st->converged = 0u;
         st->best_key = kNoMove;
+        for (int v = 0; v < kOrSlots; ++v) st->or_key[v] = kNoMove;
     }
 }
 
 cudaError_t launch_resume_descent(const TourBufs& T, cudaStream_t s) {
     return launch_chained(resume_descent_kernel, 1, 1, 0, s, T.st);
+}
+
+cudaError_t launch_apply_nbr_move(const TourBufs& T, cudaStream_t s) {
+    return launch_chained(apply_nbr_move_kernel, grid_for(T.n), kThreads, 0, s, T);
 }
 
 cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s) {

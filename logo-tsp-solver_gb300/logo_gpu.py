@@ -33,6 +33,7 @@ ROUTE_IO_COPY = 1
 ROUTE_IO_DIRECT = 2
 SEARCH_EXHAUSTIVE = 0
 SEARCH_NEIGHBOUR = 1
+SEARCH_NEIGHBOUR_OROPT = 2
 START_GIVEN = 0
 START_NN = 1
 START_MF = 2

@@ -332,8 +332,16 @@ uint64_t lo_tour_length(const float *xy, const uint32_t *route, uint32_t n)
 
 /* src/solvers/twoOptLocalSolver.cpp:22-64; each sweep on `threads` pthreads
  * (the same move: the parallel sweep keeps the lowest-(delta, i, j) rule). */
+static void nbr_candidates(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
+                           const uint32_t *nbr, uint32_t k, int oropt, int threads,
+                           uint64_t *key, uint64_t *or_key);
 static uint64_t nbr_sweep(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
-                          const uint32_t *nbr, uint32_t k);
+                          const uint32_t *nbr, uint32_t k, uint32_t lo, uint32_t hi);
+static void or_sweep(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
+                     const uint32_t *nbr, uint32_t k, uint32_t lo, uint32_t hi,
+                     uint64_t *or_key);
+static void apply_oropt(uint32_t *route, uint32_t n, uint32_t s, uint32_t L, uint32_t p,
+                        int rev, uint32_t *tmp);
 
 /* With nbr (k cities per city), the neighbour phase of LOGO_SEARCH_NEIGHBOUR
  * comes first: moves from nbr_sweep until none improves, then the full
@@ -342,7 +350,7 @@ static uint64_t nbr_sweep(const ordered_t *o, const uint32_t *route, const uint3
 static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
                             uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
                             int threads, const uint32_t *nbr, uint32_t k,
-                            uint64_t *nbr_moves)
+                            uint64_t *nbr_moves, int oropt)
 {
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
     int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(n + 1));
@@ -365,7 +373,21 @@ static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
             for (uint32_t q = 1; q < n; q++)
                 o.e[q] = lo_dist(o.x[q - 1], o.y[q - 1], o.x[q], o.y[q]);
             o.e[0] = lo_dist(o.x[n - 1], o.y[n - 1], o.x[0], o.y[0]);
-            uint64_t key = nbr_sweep(&o, route, pos, nbr, k);
+            uint64_t key;
+            uint64_t ok[5];
+            int slot = -1;
+            nbr_candidates(&o, route, pos, nbr, k, oropt, threads, &key, ok);
+            if (oropt) {
+                /* lowest delta; ties to the 2-opt move, then to the lower slot */
+                for (int v = 0; v < 5; v++) {
+                    if (ok[v] == UINT64_MAX)
+                        continue;
+                    if (key == UINT64_MAX || (ok[v] >> 42) < (key >> 42)) {
+                        key = ok[v];
+                        slot = v;
+                    }
+                }
+            }
             if (key == UINT64_MAX)
                 break;
             if ((uint64_t)moves >= max_moves) {
@@ -377,10 +399,15 @@ static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
             unpack_key(key, &d, &i, &j);
             if (move_log && (uint64_t)moves < log_cap) {
                 move_log[3 * moves + 0] = d;
-                move_log[3 * moves + 1] = (int32_t)i;
+                move_log[3 * moves + 1] =
+                    slot < 0 ? (int32_t)i : -1 - (int32_t)(i + ((uint32_t)slot << 21));
                 move_log[3 * moves + 2] = (int32_t)j;
             }
-            lo_apply_move(route, n, i, j, tmp);
+            if (slot < 0)
+                lo_apply_move(route, n, i, j, tmp);
+            else
+                apply_oropt(route, n, i, slot == 0 ? 1u : (uint32_t)((slot + 3) / 2), j,
+                            slot == 2 || slot == 4, tmp);
             moves++;
         }
         free(pos);
@@ -425,14 +452,14 @@ static int64_t descend_impl(const float *xy, uint32_t *route, uint32_t n,
 int64_t lo_descend(const float *xy, uint32_t *route, uint32_t n,
                    uint64_t max_moves, int32_t *move_log, uint64_t log_cap)
 {
-    return descend_impl(xy, route, n, max_moves, move_log, log_cap, 1, NULL, 0, NULL);
+    return descend_impl(xy, route, n, max_moves, move_log, log_cap, 1, NULL, 0, NULL, 0);
 }
 
 int64_t lo_descend_mt(const float *xy, uint32_t *route, uint32_t n,
                       uint64_t max_moves, int32_t *move_log, uint64_t log_cap,
                       int threads)
 {
-    return descend_impl(xy, route, n, max_moves, move_log, log_cap, threads, NULL, 0, NULL);
+    return descend_impl(xy, route, n, max_moves, move_log, log_cap, threads, NULL, 0, NULL, 0);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -489,13 +516,13 @@ int lo_knn(const float *xy, uint32_t n, uint32_t k, uint32_t *out)
  * b + 1 <= n - 1, i.e. the two full-sweep pairs whose move creates the edge
  * between the two cities.  Lowest improving (delta, i, c) key. */
 static uint64_t nbr_sweep(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
-                          const uint32_t *nbr, uint32_t k)
+                          const uint32_t *nbr, uint32_t k, uint32_t lo, uint32_t hi)
 {
     const uint32_t n = o->n;
     const float *X = o->x, *Y = o->y;
     const int32_t *E = o->e;
     uint64_t best = UINT64_MAX;
-    for (uint32_t i = 0; i < n; i++) {
+    for (uint32_t i = lo; i < hi && i < n; i++) {
         const uint32_t t = route[i];
         for (uint32_t q = 0; q < k; q++) {
             const uint32_t p = pos[nbr[(size_t)t * k + q]];
@@ -526,10 +553,203 @@ static uint64_t nbr_sweep(const ordered_t *o, const uint32_t *route, const uint3
     return best;
 }
 
-int64_t lo_descend_nbr(const float *xy, uint32_t *route, uint32_t n, const uint32_t *nbr,
-                       uint32_t k, uint64_t max_moves, int threads, uint64_t *nbr_moves)
+typedef struct {
+    const ordered_t *o;
+    const uint32_t *route, *pos, *nbr;
+    uint32_t k, lo, hi;
+    int oropt;
+    uint64_t key, or_key[5];
+} nbr_job_t;
+
+static void *nbr_worker(void *p)
 {
-    return descend_impl(xy, route, n, max_moves, NULL, 0, threads, nbr, k, nbr_moves);
+    nbr_job_t *j = (nbr_job_t *)p;
+    j->key = nbr_sweep(j->o, j->route, j->pos, j->nbr, j->k, j->lo, j->hi);
+    for (int v = 0; v < 5; v++)
+        j->or_key[v] = UINT64_MAX;
+    if (j->oropt)
+        or_sweep(j->o, j->route, j->pos, j->nbr, j->k, j->lo, j->hi, j->or_key);
+    return NULL;
+}
+
+/* The neighbour sweep's lowest 2-opt key and Or-opt slot keys, positions
+ * split over `threads` pthreads (the minima do not depend on the split). */
+static void nbr_candidates(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
+                           const uint32_t *nbr, uint32_t k, int oropt, int threads,
+                           uint64_t *key, uint64_t *or_key)
+{
+    const uint32_t n = o->n;
+    if (threads < 1)
+        threads = 1;
+    if (threads > 64)
+        threads = 64;
+    if ((uint32_t)threads > n / 256 + 1)
+        threads = (int)(n / 256 + 1);
+    nbr_job_t jobs[64];
+    pthread_t tid[64];
+    int started[64];
+    for (int t = 0; t < threads; t++) {
+        jobs[t].o = o;
+        jobs[t].route = route;
+        jobs[t].pos = pos;
+        jobs[t].nbr = nbr;
+        jobs[t].k = k;
+        jobs[t].oropt = oropt;
+        jobs[t].lo = (uint32_t)((uint64_t)n * t / threads);
+        jobs[t].hi = (uint32_t)((uint64_t)n * (t + 1) / threads);
+        started[t] = t > 0 && pthread_create(&tid[t], NULL, nbr_worker, &jobs[t]) == 0;
+    }
+    nbr_worker(&jobs[0]);
+    for (int t = 1; t < threads; t++) {
+        if (started[t])
+            pthread_join(tid[t], NULL);
+        else
+            nbr_worker(&jobs[t]);
+    }
+    *key = UINT64_MAX;
+    for (int v = 0; v < 5; v++)
+        or_key[v] = UINT64_MAX;
+    for (int t = 0; t < threads; t++) {
+        if (jobs[t].key < *key)
+            *key = jobs[t].key;
+        for (int v = 0; v < 5; v++)
+            if (jobs[t].or_key[v] < or_key[v])
+                or_key[v] = jobs[t].or_key[v];
+    }
+}
+
+int64_t lo_descend_nbr(const float *xy, uint32_t *route, uint32_t n, const uint32_t *nbr,
+                       uint32_t k, uint64_t max_moves, int threads, uint64_t *nbr_moves,
+                       int oropt)
+{
+    return descend_impl(xy, route, n, max_moves, NULL, 0, threads, nbr, k, nbr_moves, oropt);
+}
+
+/* One step of the neighbour search on `route` without applying it: the
+ * chosen move's delta, slot (-1 for 2-opt, else the Or-opt variant) and
+ * (i, j) = (first, second field of its key); returns 0, or 1 when no
+ * candidate improves. */
+int lo_nbr_step(const float *xy, const uint32_t *route, uint32_t n, const uint32_t *nbr,
+                uint32_t k, int oropt, int32_t *delta, int32_t *slot, uint32_t *i, uint32_t *j)
+{
+    ordered_t o;
+    uint32_t *pos = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
+    if (!pos || ordered_init(&o, xy, route, n)) {
+        free(pos);
+        return -1;
+    }
+    for (uint32_t q = 0; q < n; q++)
+        pos[route[q]] = q;
+    uint64_t key;
+    uint64_t ok[5];
+    int sl = -1;
+    nbr_candidates(&o, route, pos, nbr, k, oropt, 1, &key, ok);
+    if (oropt) {
+        for (int v = 0; v < 5; v++) {
+            if (ok[v] == UINT64_MAX)
+                continue;
+            if (key == UINT64_MAX || (ok[v] >> 42) < (key >> 42)) {
+                key = ok[v];
+                sl = v;
+            }
+        }
+    }
+    ordered_free(&o);
+    free(pos);
+    if (key == UINT64_MAX)
+        return 1;
+    unpack_key(key, delta, i, j);
+    *slot = sl;
+    return 0;
+}
+
+/* Or-opt moves (LOGO_SEARCH_NEIGHBOUR_OROPT): segment [s, s+L), L = 1..3,
+ * 1 <= s, s+L <= n-1, moved into the gap after old position p (p <= s-2, or
+ * s+L <= p <= n-2), in order or reversed.  Candidates are the moves that
+ * create an edge from a segment end to one of its listed neighbours (the
+ * city at s starts every segment; the city at s+L-1 ends the one of length
+ * L).  Slot v = (L1, L2, L2 reversed, L3, L3 reversed) keeps the lowest
+ * improving pack_key(delta, s, p). */
+static void or_try(const ordered_t *o, uint32_t s, uint32_t L, int rev, uint32_t p,
+                   int32_t base, int have, uint64_t *or_key)
+{
+    const uint32_t n = o->n;
+    if (!have)
+        return;
+    if (!(p + 2 <= s || (p >= s + L && p + 2 <= n)))
+        return;
+    const uint32_t u = rev ? s + L - 1 : s, w = rev ? s : s + L - 1;
+    /* both new distances are >= 0: the first alone may already rule it out */
+    const int32_t part = base + lo_dist(o->x[p], o->y[p], o->x[u], o->y[u]) - o->e[p + 1];
+    if (part >= 0)
+        return;
+    const int32_t delta = part + lo_dist(o->x[w], o->y[w], o->x[p + 1], o->y[p + 1]);
+    if (delta < 0) {
+        const int v = L == 1 ? 0 : (int)(2 * L - 3) + (rev ? 1 : 0);
+        const uint64_t key = lo_pack_key(delta, s, p);
+        if (key < or_key[v])
+            or_key[v] = key;
+    }
+}
+
+static void or_sweep(const ordered_t *o, const uint32_t *route, const uint32_t *pos,
+                     const uint32_t *nbr, uint32_t k, uint32_t lo, uint32_t hi,
+                     uint64_t *or_key)
+{
+    const uint32_t n = o->n;
+    for (uint32_t s = lo < 1 ? 1 : lo; s < hi && s + 2 <= n; s++) {
+        int32_t base[3];
+        int have[3];
+        for (uint32_t L = 1; L <= 3; L++) {
+            have[L - 1] = s + L <= n - 1;
+            base[L - 1] = have[L - 1] ? lo_dist(o->x[s - 1], o->y[s - 1], o->x[s + L],
+                                                o->y[s + L]) - o->e[s] - o->e[s + L]
+                                      : 0;
+        }
+        for (uint32_t anchor = 0; anchor < 3; anchor++) {
+            if (anchor >= 1 && !have[anchor])
+                break;
+            const uint32_t c = route[s + anchor];
+            for (uint32_t t = 0; t < k; t++) {
+                const uint32_t q = pos[nbr[(size_t)c * k + t]];
+                if (anchor == 0) {
+                    or_try(o, s, 1, 0, q, base[0], have[0], or_key);
+                    if (q >= 1)
+                        or_try(o, s, 1, 0, q - 1, base[0], have[0], or_key);
+                    for (uint32_t L = 2; L <= 3; L++) {
+                        or_try(o, s, L, 0, q, base[L - 1], have[L - 1], or_key);
+                        if (q >= 1)
+                            or_try(o, s, L, 1, q - 1, base[L - 1], have[L - 1], or_key);
+                    }
+                } else {
+                    const uint32_t L = anchor + 1;
+                    if (q >= 1)
+                        or_try(o, s, L, 0, q - 1, base[L - 1], have[L - 1], or_key);
+                    or_try(o, s, L, 1, q, base[L - 1], have[L - 1], or_key);
+                }
+            }
+        }
+    }
+}
+
+/* The segment moves right: old[0,s) old[s+L,p] seg old[p+1,n); left:
+ * old[0,p] seg old[p+1,s) old[s+L,n); seg reversed when rev. */
+static void apply_oropt(uint32_t *route, uint32_t n, uint32_t s, uint32_t L, uint32_t p,
+                        int rev, uint32_t *tmp)
+{
+    uint32_t q = 0;
+    if (p >= s + L) {
+        for (uint32_t t = 0; t < s; t++) tmp[q++] = route[t];
+        for (uint32_t t = s + L; t <= p; t++) tmp[q++] = route[t];
+        for (uint32_t t = 0; t < L; t++) tmp[q++] = route[rev ? s + L - 1 - t : s + t];
+        for (uint32_t t = p + 1; t < n; t++) tmp[q++] = route[t];
+    } else {
+        for (uint32_t t = 0; t <= p; t++) tmp[q++] = route[t];
+        for (uint32_t t = 0; t < L; t++) tmp[q++] = route[rev ? s + L - 1 - t : s + t];
+        for (uint32_t t = p + 1; t < s; t++) tmp[q++] = route[t];
+        for (uint32_t t = s + L; t < n; t++) tmp[q++] = route[t];
+    }
+    memcpy(route, tmp, sizeof(uint32_t) * n);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -574,7 +794,8 @@ void lo_kick_double_bridge(uint32_t *route, uint32_t n, uint64_t *rng,
  * :98-99, and ends after one pass otherwise). */
 static int ils_impl(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
                     uint64_t seed, int kick_kind, uint64_t max_moves_per_descent,
-                    lo_ils_stats *stats, int threads, const uint32_t *nbr, uint32_t k)
+                    lo_ils_stats *stats, int threads, const uint32_t *nbr, uint32_t k,
+                    int oropt)
 {
     uint32_t *best = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
     uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (n + 1));
@@ -587,7 +808,7 @@ static int ils_impl(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks
     memcpy(best, route, sizeof(uint32_t) * n);
     for (uint32_t it = 0;; it++) {
         int64_t m = descend_impl(xy, route, n, max_moves_per_descent, NULL, 0, threads, nbr, k,
-                                 NULL);
+                                 NULL, oropt);
         st.descents++;
         if (m < 0) {
             rc = -1;
@@ -623,7 +844,7 @@ int lo_ils(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
            lo_ils_stats *stats)
 {
     return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats, 1,
-                    NULL, 0);
+                    NULL, 0, 0);
 }
 
 int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
@@ -631,15 +852,15 @@ int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
               lo_ils_stats *stats, int threads)
 {
     return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats,
-                    threads, NULL, 0);
+                    threads, NULL, 0, 0);
 }
 
 int lo_ils_nbr(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks, uint64_t seed,
                int kick_kind, uint64_t max_moves_per_descent, lo_ils_stats *stats,
-               int threads, const uint32_t *nbr, uint32_t k)
+               int threads, const uint32_t *nbr, uint32_t k, int oropt)
 {
     return ils_impl(xy, route, n, kicks, seed, kick_kind, max_moves_per_descent, stats,
-                    threads, nbr, k);
+                    threads, nbr, k, oropt);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -133,13 +133,18 @@ int lo_ils_mt(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks,
  * a city to one of its listed neighbours until none improves, then full
  * best-improvement sweeps (as lo_descend) to a local optimum; moves of both
  * phases count towards max_moves, *nbr_moves gets the first phase's.
- * lo_ils_nbr is lo_ils_mt with those descents. */
+ * lo_ils_nbr is lo_ils_mt with those descents.  With oropt the neighbour
+ * phase also weighs Or-opt moves (segments of 1-3 cities moved, in order or
+ * reversed, next to a listed neighbour; LOGO_SEARCH_NEIGHBOUR_OROPT). */
 int lo_knn(const float *xy, uint32_t n, uint32_t k, uint32_t *out);
 int64_t lo_descend_nbr(const float *xy, uint32_t *route, uint32_t n, const uint32_t *nbr,
-                       uint32_t k, uint64_t max_moves, int threads, uint64_t *nbr_moves);
+                       uint32_t k, uint64_t max_moves, int threads, uint64_t *nbr_moves,
+                       int oropt);
+int lo_nbr_step(const float *xy, const uint32_t *route, uint32_t n, const uint32_t *nbr,
+                uint32_t k, int oropt, int32_t *delta, int32_t *slot, uint32_t *i, uint32_t *j);
 int lo_ils_nbr(const float *xy, uint32_t *route, uint32_t n, uint32_t kicks, uint64_t seed,
                int kick_kind, uint64_t max_moves_per_descent, lo_ils_stats *stats,
-               int threads, const uint32_t *nbr, uint32_t k);
+               int threads, const uint32_t *nbr, uint32_t k, int oropt);
 
 /* Nearest-neighbour start tour, initRoute_KD_NN
  * (src/utils/kdtree_utils.c:279-301): start at city 0, repeatedly go to the

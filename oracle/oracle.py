@@ -88,12 +88,15 @@ def lib():
         L.lo_knn.argtypes = [_f32p, ctypes.c_uint32, ctypes.c_uint32, _u32p]
         L.lo_descend_nbr.restype = ctypes.c_int64
         L.lo_descend_nbr.argtypes = [_f32p, _u32p, ctypes.c_uint32, _u32p, ctypes.c_uint32,
-                                     ctypes.c_uint64, ctypes.c_int, _u64p]
+                                     ctypes.c_uint64, ctypes.c_int, _u64p, ctypes.c_int]
+        L.lo_nbr_step.restype = ctypes.c_int
+        L.lo_nbr_step.argtypes = [_f32p, _u32p, ctypes.c_uint32, _u32p, ctypes.c_uint32,
+                                  ctypes.c_int, _i32p, _i32p, _u32p, _u32p]
         L.lo_ils_nbr.restype = ctypes.c_int
         L.lo_ils_nbr.argtypes = [_f32p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
                                  ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
                                  ctypes.POINTER(IlsStats), ctypes.c_int, _u32p,
-                                 ctypes.c_uint32]
+                                 ctypes.c_uint32, ctypes.c_int]
         L.lo_ils_batch.restype = ctypes.c_int
         L.lo_ils_batch.argtypes = [_f32p, _u32p, _u64p, _u32p, _u64p, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
@@ -172,7 +175,7 @@ def knn(xy, k):
     return out
 
 
-def descend_nbr(xy, route, k=8, max_moves=None, threads=1, stop_at_limit=False):
+def descend_nbr(xy, route, k=8, max_moves=None, threads=1, stop_at_limit=False, oropt=False):
     """Neighbour-list search (neighbour moves, then full sweeps): returns
     (final_route, moves, moves of the neighbour phase).  stop_at_limit: a
     descent that still has moves after max_moves returns its state there
@@ -185,7 +188,7 @@ def descend_nbr(xy, route, k=8, max_moves=None, threads=1, stop_at_limit=False):
         max_moves = 64 * n * n + 1024
     nm = ctypes.c_uint64(0)
     m = lib().lo_descend_nbr(pxy, r.ctypes.data_as(_u32p), n, nb.ctypes.data_as(_u32p), k,
-                             max_moves, max(1, int(threads)), ctypes.byref(nm))
+                             max_moves, max(1, int(threads)), ctypes.byref(nm), int(oropt))
     if m < 0:
         if not stop_at_limit:
             raise RuntimeError("oracle descent exceeded max_moves")
@@ -193,7 +196,25 @@ def descend_nbr(xy, route, k=8, max_moves=None, threads=1, stop_at_limit=False):
     return r, m, nm.value
 
 
-def ils_nbr(xy, route, kicks, seed, kind=KICK_SEGMENT, k=8, max_moves=None, threads=1):
+def nbr_step(xy, route, k=8, oropt=False, nb=None):
+    """The move one neighbour-search step would apply: (delta, slot, i, j)
+    with slot -1 for 2-opt, else the Or-opt variant; None if none improves."""
+    if nb is None:
+        nb = knn(xy, k)
+    nb = np.ascontiguousarray(nb, dtype=np.uint32)
+    xy, pxy = _f32(xy)
+    route, pr = _u32(route)
+    d, sl = ctypes.c_int32(), ctypes.c_int32()
+    i, j = ctypes.c_uint32(), ctypes.c_uint32()
+    rc = lib().lo_nbr_step(pxy, pr, len(route), nb.ctypes.data_as(_u32p), k, int(oropt),
+                           ctypes.byref(d), ctypes.byref(sl), ctypes.byref(i), ctypes.byref(j))
+    if rc < 0:
+        raise MemoryError("oracle allocation failed")
+    return None if rc == 1 else (d.value, sl.value, i.value, j.value)
+
+
+def ils_nbr(xy, route, kicks, seed, kind=KICK_SEGMENT, k=8, max_moves=None, threads=1,
+            oropt=False):
     """ils() with the neighbour-list search in every descent."""
     nb = np.ascontiguousarray(knn(xy, k))
     xy, pxy = _f32(xy)
@@ -203,7 +224,8 @@ def ils_nbr(xy, route, kicks, seed, kind=KICK_SEGMENT, k=8, max_moves=None, thre
         max_moves = 64 * n * n + 1024
     st = IlsStats()
     rc = lib().lo_ils_nbr(pxy, r.ctypes.data_as(_u32p), n, kicks, seed, kind, max_moves,
-                          ctypes.byref(st), max(1, int(threads)), nb.ctypes.data_as(_u32p), k)
+                          ctypes.byref(st), max(1, int(threads)), nb.ctypes.data_as(_u32p), k,
+                          int(oropt))
     if rc:
         raise RuntimeError("oracle ILS descent exceeded max_moves")
     return r, {f: getattr(st, f) for f, _ in IlsStats._fields_}

@@ -6,8 +6,9 @@ tests/test_neighbour_search.py).
 * Descents: final tour, move count and the neighbour phase's moves equal
   the oracle's, on uniform, clustered and integer-grid instances (equal
   distances, duplicate points), from random and nearest-neighbour tours,
-  with the MUFU screen (n = 1000, 5000) and the boxed screen (n = 24,000)
-  finishing the descent, and with lists of 4, 8 and 16 cities.
+  with the MUFU screen (n = 1000, 5000) and the boxed screen (n = 24,000,
+  nearest-neighbour starts) finishing the descent, and with lists of 4, 5,
+  8 and 16 cities.
 * With lists of every other city (n = 17, k = 16) the search is the
   reference's exhaustive descent, move for move.
 * A move limit stops the search where the oracle's stops.
@@ -15,6 +16,8 @@ tests/test_neighbour_search.py).
   ILS graph) equals the oracle's ILS with the same descents.
 * Switching a context back to the exhaustive search gives the reference's
   descent again.
+* The same with Or-opt candidates (LOGO_SEARCH_NEIGHBOUR_OROPT, oracle
+  lo_descend_nbr / lo_ils_nbr with oropt): descents, a move limit and ILS.
 """
 import os
 
@@ -37,18 +40,21 @@ def _case(lg, inst, kind, n, seed):
     return xy, r
 
 
-@pytest.mark.parametrize("kind,n,seed,k", [
-    ("uniform", 1000, 1, 8), ("clustered", 1000, 2, 4), ("grid", 1000, 3, 16),
-    ("uniform", 5000, 4, 8), ("grid", 5000, 5, 8), ("clustered", 24000, 6, 8),
-    ("uniform", 24000, 7, 8),
+@pytest.mark.parametrize("kind,n,seed,k,oropt", [
+    ("uniform", 1000, 1, 8, False), ("clustered", 1000, 2, 4, False), ("grid", 1000, 3, 16, False),
+    ("uniform", 5000, 4, 8, False), ("grid", 5000, 5, 8, False), ("clustered", 24000, 6, 8, False),
+    ("uniform", 24000, 8, 8, False),
+    ("uniform", 1000, 1, 8, True), ("grid", 1000, 3, 5, True), ("clustered", 5000, 8, 8, True),
+    ("grid", 3000, 9, 16, True), ("uniform", 12000, 10, 8, True),
 ])
-def test_descent_matches_the_oracle(lg, inst, oracle_mod, kind, n, seed, k):
+def test_descent_matches_the_oracle(lg, inst, oracle_mod, kind, n, seed, k, oropt):
     xy, r = _case(lg, inst, kind, n, seed)
-    want, m, nm = oracle_mod.descend_nbr(xy, r, k=k, threads=THREADS)
+    want, m, nm = oracle_mod.descend_nbr(xy, r, k=k, threads=THREADS, oropt=oropt)
+    mode = lg.SEARCH_NEIGHBOUR_OROPT if oropt else lg.SEARCH_NEIGHBOUR
     with lg.Solver(xy) as s:
-        s.set_search(lg.SEARCH_NEIGHBOUR, k)
+        s.set_search(mode, k)
         info = s.info()
-        assert info["search"] == lg.SEARCH_NEIGHBOUR and info["search_neighbours"] == k
+        assert info["search"] == mode and info["search_neighbours"] == k
         got, st = s.optimize(r)
         assert st["moves"] == m
         assert st["final_length"] == oracle_mod.tour_length(xy, want)
@@ -77,24 +83,27 @@ def test_full_lists_are_the_exhaustive_descent(lg, inst, oracle_mod):
         assert np.array_equal(got, want) and st["moves"] == m
 
 
-@pytest.mark.parametrize("limit", [1, 7, 40])
-def test_move_limit(lg, inst, oracle_mod, limit):
+@pytest.mark.parametrize("limit,oropt", [(1, False), (7, False), (40, False), (1, True),
+                                         (33, True)])
+def test_move_limit(lg, inst, oracle_mod, limit, oropt):
     xy, r = _case(lg, inst, "uniform", 3000, 11)
     want, m, _ = oracle_mod.descend_nbr(xy, r, k=8, max_moves=limit, threads=THREADS,
-                                       stop_at_limit=True)
+                                       stop_at_limit=True, oropt=oropt)
     with lg.Solver(xy) as s:
-        s.set_search(lg.SEARCH_NEIGHBOUR)
+        s.set_search(lg.SEARCH_NEIGHBOUR_OROPT if oropt else lg.SEARCH_NEIGHBOUR)
         got, st = s.optimize(r, max_moves=limit)
     assert st["moves"] == m == limit
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("n,kicks,kind", [(2000, 12, 1), (3000, 8, 0), (20000, 4, 1)])
-def test_ils_matches_the_oracle(lg, inst, oracle_mod, n, kicks, kind):
+@pytest.mark.parametrize("n,kicks,kind,oropt", [(2000, 12, 1, False), (3000, 8, 0, False),
+                                                (20000, 4, 1, False), (2000, 12, 1, True),
+                                                (8000, 4, 0, True)])
+def test_ils_matches_the_oracle(lg, inst, oracle_mod, n, kicks, kind, oropt):
     xy, r = _case(lg, inst, "clustered", n, 20 + n)
-    want, wst = oracle_mod.ils_nbr(xy, r, kicks, 5, kind, k=8, threads=THREADS)
+    want, wst = oracle_mod.ils_nbr(xy, r, kicks, 5, kind, k=8, threads=THREADS, oropt=oropt)
     with lg.Solver(xy) as s:
-        s.set_search(lg.SEARCH_NEIGHBOUR)
+        s.set_search(lg.SEARCH_NEIGHBOUR_OROPT if oropt else lg.SEARCH_NEIGHBOUR)
         got, st = s.ils(r, kicks, 5, kind)
     assert st["final_length"] == wst["best_length"]
     assert st["moves"] == wst["moves"] and st["accepted"] == wst["accepted"]

@@ -56,3 +56,43 @@ def test_short_lists_end_at_a_local_optimum(inst, oracle_mod):
         assert oracle_mod.best_move(xy, got) == (0, 0, 0)
         assert 0 < nm <= m
         assert oracle_mod.tour_length(xy, got) < oracle_mod.tour_length(xy, r)
+
+
+def test_oropt_steps_change_the_length_by_their_delta(inst, oracle_mod):
+    """Every step of the search with Or-opt moves changes the tour length by
+    exactly the delta it was chosen with, keeps a permutation, and Or-opt
+    moves of every variant (segment lengths 1-3, in order and reversed,
+    moved left and right) occur."""
+    seen = set()
+    for n, seed in ((400, 1), (250, 2), (120, 3)):
+        xy = inst.uniform_f32(n, seed, 1.0e4)
+        r = inst.random_tour(n, seed)
+        nb = oracle_mod.knn(xy, 8)
+        for _ in range(400):
+            step = oracle_mod.nbr_step(xy, r, 8, oropt=True, nb=nb)
+            if step is None:
+                break
+            d, slot, i, j = step
+            before = oracle_mod.tour_length(xy, r)
+            r2, m, _ = oracle_mod.descend_nbr(xy, r, 8, max_moves=1, stop_at_limit=True,
+                                              oropt=True)
+            assert m == 1 and oracle_mod.check_tour(r2, n)
+            assert oracle_mod.tour_length(xy, r2) - before == d < 0
+            if slot >= 0:
+                seen.add((slot, j > i))
+            r = r2
+    assert {s for s, _ in seen} == {0, 1, 2, 3, 4}
+    assert {right for _, right in seen} == {False, True}
+
+
+def test_oropt_search_ends_at_a_local_optimum(inst, oracle_mod):
+    for xy, r in ((inst.uniform_f32(1500, 6, 1.0e4), inst.random_tour(1500, 6)),
+                  (inst.clustered(1200, 7, side=1.0e6, clusters=8), None)):
+        if r is None:
+            r = np.arange(len(xy), dtype=np.uint32)
+        got, m, nm = oracle_mod.descend_nbr(xy, r, k=8, threads=4, oropt=True)
+        plain, _, _ = oracle_mod.descend_nbr(xy, r, k=8, threads=4)
+        assert oracle_mod.check_tour(got, len(xy))
+        assert oracle_mod.best_move(xy, got) == (0, 0, 0)
+        assert 0 < nm <= m
+        assert oracle_mod.tour_length(xy, got) < oracle_mod.tour_length(xy, plain)

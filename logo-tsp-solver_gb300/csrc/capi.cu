@@ -671,9 +671,13 @@ logo_status graph_descent(logo_ctx* c, uint64_t max_moves, bool partial_ok, uint
             const TourBufs T = bufs(c);
             for (uint64_t k = 0; k < left; ++k) {
                 CK(c, nbr ? launch_nbr_sweep(N, c->stream) : launch_sweep(L, c->stream));
-                CK(c, nbr ? launch_nbr_apply(c, T, c->stream) : launch_apply_move(T, c->stream));
+                // the last full-sweep step also hands the tour back (direct mode)
+                uint32_t* out = !nbr && route_out && k + 1 == left ? route_out : nullptr;
+                CK(c, nbr ? launch_nbr_apply(c, T, c->stream)
+                          : launch_apply_move(T, c->stream, out));
+                stored = stored || out != nullptr;
             }
-            if (route_out) {
+            if (route_out && !stored) {
                 logo_status s = enqueue_route_out(c, route_out, false);
                 if (s != LOGO_OK) return s;
                 stored = true;

@@ -176,8 +176,9 @@ cudaError_t launch_store_route(const TourBufs& T, uint32_t* dst, bool best, cuda
 // Prepares *st for a new descent: cur = 0 kept, counters cleared.
 cudaError_t launch_reset_descent(const TourBufs& T, unsigned long long max_moves,
                                  cudaStream_t s);
-// Applies the move in st->best_key (or marks convergence).
-cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s);
+// Applies the move in st->best_key (or marks convergence); with out, also
+// writes the resulting current tour there (moved or not).
+cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s, uint32_t* out = nullptr);
 // The same for the neighbour search with Or-opt moves: the best of
 // st->best_key and st->or_key[].
 cudaError_t launch_apply_nbr_move(const TourBufs& T, cudaStream_t s);

@@ -150,7 +150,8 @@ __device__ __forceinline__ void gather_tour(const OrderedCity* __restrict__ Qs,
                                             const uint32_t* __restrict__ Rs,
                                             OrderedCity* __restrict__ Qd,
                                             uint32_t* __restrict__ Rd, uint32_t n,
-                                            uint32_t* __restrict__ pos, Src src) {
+                                            uint32_t* __restrict__ pos, Src src,
+                                            uint32_t* out = nullptr) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += gridDim.x * blockDim.x) {
         const uint32_t s = src(k);
@@ -165,20 +166,30 @@ __device__ __forceinline__ void gather_tour(const OrderedCity* __restrict__ Qs,
         Qd[k] = o;
         const uint32_t id = Rs[s];
         Rd[k] = id;
+        if (out) out[k] = id;
         if (pos) pos[min(id, n - 1)] = k;
     }
 }
 
-__global__ void apply_move_kernel(TourBufs T) {
+// out (optional): the caller's route buffer, written with the tour this
+// launch leaves (moved, or unchanged when there is no move) -- the last step
+// of a short descent hands its result back without a separate store.
+__global__ void apply_move_kernel(TourBufs T, uint32_t* out) {
     chain_wait();
     chain_release();
     DevState* st = T.st;
-    if (*(volatile unsigned int*)&st->converged) return;
-    const uint64_t key = *(volatile unsigned long long*)&st->best_key;
     const uint32_t cur = *(volatile unsigned int*)&st->cur;
     const uint32_t n = T.n;
+    const bool done = *(volatile unsigned int*)&st->converged;
+    const uint64_t key = done ? kNoMove : *(volatile unsigned long long*)&st->best_key;
     if (key == kNoMove) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (out) {
+            const uint32_t* R = cur ? T.route[1] : T.route[0];
+            for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+                 k += gridDim.x * blockDim.x)
+                out[k] = R[k];
+        }
+        if (!done && blockIdx.x == 0 && threadIdx.x == 0) {
             st->converged = 1;
             st->sweeps += 1;
         }
@@ -187,6 +198,12 @@ __global__ void apply_move_kernel(TourBufs T) {
     // reported move (i, j+1): p = i < q = j+1 (twoOptLocalSolver.cpp:41-48)
     const uint32_t p = key_i(key), q = key_j(key);
     if (!(p >= 1 && q < n && q >= p + 2)) {
+        if (out) {
+            const uint32_t* R = cur ? T.route[1] : T.route[0];
+            for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+                 k += gridDim.x * blockDim.x)
+                out[k] = R[k];
+        }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             atomicOr(&st->status, kErrBadKey);
             st->converged = 1;
@@ -195,7 +212,7 @@ __global__ void apply_move_kernel(TourBufs T) {
     }
     gather_tour(cur ? T.Q[1] : T.Q[0], cur ? T.route[1] : T.route[0], cur ? T.Q[0] : T.Q[1],
                 cur ? T.route[0] : T.route[1], n, T.pos,
-                [=] __device__(uint32_t k) { return rotrev_src(k, p, q, n); });
+                [=] __device__(uint32_t k) { return rotrev_src(k, p, q, n); }, out);
     if (last_block_done(&st->done_blocks)) {
         const unsigned long long m = st->moves;
         if (st->move_log && m < st->log_cap) {
@@ -472,8 +489,8 @@ cudaError_t launch_apply_nbr_move(const TourBufs& T, cudaStream_t s) {
     return launch_chained(apply_nbr_move_kernel, grid_for(T.n), kThreads, 0, s, T);
 }
 
-cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s) {
-    return launch_chained(apply_move_kernel, grid_for(T.n), kThreads, 0, s, T);
+cudaError_t launch_apply_move(const TourBufs& T, cudaStream_t s, uint32_t* out) {
+    return launch_chained(apply_move_kernel, grid_for(T.n), kThreads, 0, s, T, out);
 }
 cudaError_t launch_tour_length(const TourBufs& T, cudaStream_t s) {
     tour_length_kernel<<<grid_for(T.n), kThreads, 0, s>>>(T);

@@ -122,3 +122,21 @@ def test_switching_back_to_the_exhaustive_search(lg, inst, oracle_mod):
     assert np.array_equal(got, want) and st["moves"] == m
     with lg.Solver(xy) as s, pytest.raises(lg.LogoError):
         s.set_search(lg.SEARCH_NEIGHBOUR, 17)
+
+
+def test_tiny_tours_in_both_neighbour_modes(lg, inst, oracle_mod):
+    """3 to 12 cities (fewer other cities than list slots, segments that do
+    not fit): descents and a short ILS equal the oracle's in both modes."""
+    for n in range(3, 13):
+        for seed in (1, 2):
+            xy = inst.uniform_int(n, 300 + 10 * n + seed)
+            r = inst.random_tour(n, 400 + 10 * n + seed)
+            for oropt in (False, True):
+                want, m, _ = oracle_mod.descend_nbr(xy, r, k=8, oropt=oropt)
+                wils, wst = oracle_mod.ils_nbr(xy, r, 5, 3, 1, k=8, oropt=oropt)
+                with lg.Solver(xy) as s:
+                    s.set_search(lg.SEARCH_NEIGHBOUR_OROPT if oropt else lg.SEARCH_NEIGHBOUR)
+                    got, st = s.optimize(r)
+                    gils, gst = s.ils(r, 5, 3, lg.KICK_DOUBLE_BRIDGE)
+                assert np.array_equal(got, want) and st["moves"] == m, (n, oropt)
+                assert np.array_equal(gils, wils) and gst["final_length"] == wst["best_length"]

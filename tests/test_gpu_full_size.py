@@ -11,7 +11,13 @@ sweep so that a 5e9-pair sweep takes well under a second of host time:
   sweep-throughput case, about 5e11 pairs);
 * a reduced large-instance run (n = 20,000 Gaussian mixture, nearest-neighbour
   start, descent + 20 double-bridge kicks through logo_ils) against the
-  oracle's ILS: best tour, length, moves and acceptances.
+  oracle's ILS: best tour, length, moves and acceptances;
+* the neighbour-list search (LOGO_SEARCH_NEIGHBOUR, 8 nearest cities) on a
+  25,000-city Gaussian mixture from its nearest-neighbour tour (the boxed
+  screen finishes the descent): the whole descent against the oracle's
+  restatement (tour, moves, length).  At the benchmark's 100,000 cities the
+  oracle needs about 700 full sweeps after the neighbour phase, several
+  minutes of host time.
 
 The reference loop these follow is CPUSolver::optimizeStep
 (src/solvers/cpuSolver.cpp:104-146) inside TwoOptLocalSolver::optimize
@@ -79,4 +85,18 @@ def test_reduced_large_instance_ils(lg, inst, oracle_mod):
         got, st = s.ils(r0, 20, 77, lg.KICK_DOUBLE_BRIDGE)
     assert st["final_length"] == wst["best_length"]
     assert st["moves"] == wst["moves"] and st["accepted"] == wst["accepted"]
+    assert np.array_equal(got, want)
+
+
+def test_neighbour_search_descent_on_a_boxed_size_instance(lg, inst, oracle_mod):
+    n = 25000
+    xy = inst.clustered(n, 12, side=1.0e6, clusters=50, sigma_frac=0.01)
+    r0 = lg.nn_tour(xy, 0)
+    want, m, nm = oracle_mod.descend_nbr(xy, r0, k=8, threads=THREADS)
+    with lg.Solver(xy) as s:
+        assert s.info()["variant"] == lg.SWEEP_BOXED
+        s.set_search(lg.SEARCH_NEIGHBOUR, 8)
+        got, st = s.optimize(r0)
+    assert st["moves"] == m and nm > 2500 and m > nm
+    assert st["final_length"] == oracle_mod.tour_length(xy, want)
     assert np.array_equal(got, want)

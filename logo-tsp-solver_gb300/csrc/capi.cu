@@ -42,6 +42,7 @@ struct logo_ctx {
     uint32_t nbr_list_k = 0;                // length d_nbr_search was built with
     cudaGraphExec_t nbr_chunk_exec = nullptr;  // nbr_chunk_steps x (neighbour sweep, apply)
     uint32_t nbr_chunk_steps = 32;
+    int nbr_coop_grid = 0;        // CTAs of the cooperative neighbour phase (0: graphs)
     bool pageable_ok = false;     // the device reads and writes pageable host memory
     float4* d_wbox = nullptr;     // per-window boxes and largest edges (boxed sweep)
     float* d_wmax = nullptr;
@@ -117,6 +118,10 @@ NbrLaunch nbr_args(const logo_ctx* c) {
     L.Q1 = c->d_Q[1];
     L.R0 = c->d_route[0];
     L.R1 = c->d_route[1];
+    L.Q0w = c->d_Q[0];
+    L.Q1w = c->d_Q[1];
+    L.R0w = c->d_route[0];
+    L.R1w = c->d_route[1];
     L.pos = c->d_pos;
     L.nbr = c->d_nbr_search;
     L.K = c->search_k;
@@ -328,6 +333,10 @@ logo_status rebuild(logo_ctx* c) {
 // Neighbour lists and exact positions for LOGO_SEARCH_NEIGHBOUR (host grid
 // search, once per list length); graphs are rebuilt by the caller.
 logo_status prepare_search(logo_ctx* c) {
+    c->nbr_coop_grid =
+        coop_nbr_grid(c->n, c->search == LOGO_SEARCH_NEIGHBOUR_OROPT, c->device);
+    if (c->nbr_coop_grid > 0 && !c->d_coop)
+        CK(c, cudaMalloc(&c->d_coop, sizeof(CoopSync)));
     if (!c->d_pos) {
         CK(c, cudaMalloc(&c->d_pos, sizeof(uint32_t) * c->n));
         CK(c, cudaMemset(c->d_pos, 0, sizeof(uint32_t) * c->n));
@@ -631,9 +640,18 @@ logo_status run_descent(logo_ctx* c, uint64_t max_moves, uint64_t* moves_out,
         if (!c->h_st->converged && !c->h_st->status)
             return fail(c, LOGO_ERR_DEVICE_FAULT, "cooperative descent did not finish");
     } else if (c->search != LOGO_SEARCH_EXHAUSTIVE) {
-        // neighbour sweeps until no candidate improves, then full sweeps
-        logo_status s = graph_descent(c, max_moves, reset, moves0, moves0, nullptr, nullptr,
-                                      true);
+        // neighbour sweeps until no candidate improves (one cooperative
+        // launch where available), then full sweeps
+        logo_status s;
+        if (c->nbr_coop_grid > 0 && c->descent_mode != LOGO_DESCENT_GRAPH) {
+            CK(c, cudaMemsetAsync(c->d_coop, 0xFF, sizeof(CoopSync), c->stream));
+            CK(c, cudaMemsetAsync(c->d_coop, 0, 2 * sizeof(unsigned int), c->stream));
+            std::lock_guard<std::mutex> lk(coop_lock(c->device));
+            CK(c, launch_coop_nbr(nbr_args(c), c->d_coop, c->nbr_coop_grid, c->stream));
+            s = read_state(c);
+        } else {
+            s = graph_descent(c, max_moves, reset, moves0, moves0, nullptr, nullptr, true);
+        }
         if (s != LOGO_OK) return s;
         if (!c->h_st->status && !c->h_st->bad_route) {
             CK(c, launch_resume_descent(bufs(c), c->stream));

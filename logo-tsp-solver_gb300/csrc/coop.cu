@@ -27,6 +27,7 @@
 // leaves the loop, so the others give up too and the launch ends.
 #include "logo_device.cuh"
 #include "logo_internal.h"
+#include "neighbour_core.cuh"
 #include "sweep_core.cuh"
 
 namespace logo {
@@ -70,6 +71,10 @@ __device__ bool grid_barrier(CoopSync* cs, unsigned int nblocks, DevState* st, b
                 __nanosleep(32);
             }
         }
+        // as cooperative groups' grid sync: after the barrier every thread
+        // sees every global write made before it (the cooperative neighbour
+        // phase reads the tour other SMs just moved)
+        __threadfence();
         *ok_s = ok;
     }
     __syncthreads();
@@ -369,6 +374,152 @@ cudaError_t launch_coop_t(const CoopArgs& A, int grid, cudaStream_t s) {
 // Test hook for the bounded wait: one CTA waits at a barrier sized for two,
 // which nothing else will reach; the wait gives up after its budget and sets
 // kErrTimeout in st->status.
+// The neighbour phase of LOGO_SEARCH_NEIGHBOUR(_OROPT) as one cooperative
+// launch over tours of any size (the tour stays in global memory, buffers
+// cur and cur ^ 1 as for the multi-kernel path): per move, every CTA
+// evaluates the candidates of its positions (neighbour_core.cuh) into the
+// move's key slots, one grid barrier, every CTA reads the same best move
+// (the rule of apply_nbr_move_kernel) and gathers its share of the moved
+// tour (Q, route, pos), a second barrier, and the buffers swap.  Slot s % 3
+// of sweep s is cleared by CTA 0 during sweep s - 1, after every CTA read it
+// for sweep s - 3.  DevState at the end is what the sweep and apply kernels
+// leave after the same moves: moves, total_moves, sweeps and nbr_sweeps
+// (one per sweep, the converging one included), converged, cur, the move
+// log, kErrMoveLimit at max_moves, kErrBadKey on an out-of-range key.
+#ifndef LOGO_COOP_LD
+#define LOGO_COOP_LD kLdCoherent
+#endif
+constexpr int kCoopLd = LOGO_COOP_LD;
+
+template <bool OR, int NT>
+__global__ void __launch_bounds__(NT) coop_nbr_kernel(NbrLaunch L, CoopSync* cs) {
+    __shared__ unsigned long long red[NT / 32];
+    __shared__ unsigned long long red_or[OR ? kOrSlots : 1][NT / 32];
+    __shared__ bool ok_s;
+    DevState* st = L.st;
+    const uint32_t n = L.n;
+    const unsigned int nblocks = gridDim.x;
+    uint32_t cur = *(volatile unsigned int*)&st->cur;
+    const unsigned long long max_moves = *(volatile unsigned long long*)&st->max_moves;
+    unsigned long long moves = *(volatile unsigned long long*)&st->moves;
+    const unsigned long long moves0 = moves;
+    const bool start_done = *(volatile unsigned int*)&st->converged;
+    uint32_t sweeps = 0;
+    bool limit = false, bad = false, timeout = false;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t sw = 0; !start_done; ++sw) {
+        const uint32_t slot = sw % 3;
+        const OrderedCity* Q = cur ? L.Q1 : L.Q0;
+        const uint32_t* R = cur ? L.R1 : L.R0;
+        uint64_t best = kNoMove;
+        uint64_t bo[kOrSlots];
+#pragma unroll
+        for (int v = 0; v < kOrSlots; ++v) bo[v] = kNoMove;
+        for (uint32_t i = blockIdx.x * NT + threadIdx.x; i < n; i += nblocks * NT)
+            nbr_position<OR, kCoopLd>(i, Q, R, L.pos, L.nbr, L.K, n, L.margin, best, bo);
+        best = warp_min_u64(best);
+        if (lane == 0) red[warp] = best;
+        if (OR) {
+#pragma unroll
+            for (int v = 0; v < kOrSlots; ++v) {
+                const uint64_t m = warp_min_u64(bo[v]);
+                if (lane == 0) red_or[v][warp] = m;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t m = red[0];
+            for (int w = 1; w < NT / 32; ++w) m = red[w] < m ? red[w] : m;
+            if (m != kNoMove) atomicMin(&cs->slot[slot], (unsigned long long)m);
+            if (OR) {
+                for (int v = 0; v < kOrSlots; ++v) {
+                    uint64_t mv = red_or[v][0];
+                    for (int w = 1; w < NT / 32; ++w) mv = red_or[v][w] < mv ? red_or[v][w] : mv;
+                    if (mv != kNoMove) atomicMin(&cs->or_slot[slot][v], (unsigned long long)mv);
+                }
+            }
+            if (blockIdx.x == 0) {  // the next sweep's slots
+                const uint32_t nx = (sw + 1) % 3;
+                cs->slot[nx] = kNoMove;
+                for (int v = 0; v < kOrSlots; ++v) cs->or_slot[nx][v] = kNoMove;
+            }
+        }
+        ++sweeps;
+        if (!grid_barrier(cs, nblocks, st, &ok_s)) {
+            timeout = true;
+            break;
+        }
+        // the move: lowest delta, ties to the 2-opt move, then the lower slot
+        uint64_t key = ld_acquire_u64(&cs->slot[slot]);
+        int vslot = -1;
+        if (OR) {
+            for (int v = 0; v < kOrSlots; ++v) {
+                const uint64_t k = ld_acquire_u64(&cs->or_slot[slot][v]);
+                if (k != kNoMove && (key == kNoMove || key_delta(k) < key_delta(key))) {
+                    key = k;
+                    vslot = v;
+                }
+            }
+        }
+        if (key == kNoMove) break;  // converged (every CTA reads the same keys)
+        const uint32_t a = key_i(key), b = key_j(key);
+        const uint32_t Lg = vslot >= 0 ? or_len(vslot) : 0u;
+        const bool rev = vslot >= 0 && or_rev(vslot);
+        const bool ok = vslot < 0 ? (a >= 1 && b < n && b >= a + 2)
+                                  : (a >= 1 && a + Lg <= n - 1 &&
+                                     (b + 2 <= a || (b >= a + Lg && b + 2 <= n)));
+        if (!ok) {
+            bad = true;
+            break;
+        }
+        const OrderedCity* Qs = Q;
+        OrderedCity* Qd = cur ? L.Q0w : L.Q1w;
+        uint32_t* Rd = cur ? L.R0w : L.R1w;
+        for (uint32_t k = blockIdx.x * NT + threadIdx.x; k < n; k += nblocks * NT) {
+            const uint32_t km = k == 0 ? n - 1 : k - 1;
+            const uint32_t src = vslot < 0 ? rotrev_src(k, a, b, n) : oropt_src(k, a, Lg, b, rev);
+            const uint32_t srcm =
+                vslot < 0 ? rotrev_src(km, a, b, n) : oropt_src(km, a, Lg, b, rev);
+            const OrderedCity qa = ld_city<kCoopLd>(Qs + src), qb = ld_city<kCoopLd>(Qs + srcm);
+            OrderedCity o;
+            o.x = qa.x;
+            o.y = qa.y;
+            o.e = (float)exact_dist(qb.x, qb.y, qa.x, qa.y);
+            o.pad = 0.f;
+            Qd[k] = o;
+            const uint32_t id = ld_u32<kCoopLd>(R + src);
+            Rd[k] = id;
+            L.pos[min(id, n - 1)] = k;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0 && st->move_log && moves < st->log_cap) {
+            st->move_log[3 * moves + 0] = key_delta(key);
+            st->move_log[3 * moves + 1] = vslot < 0 ? (int)a : -1 - (int)(a + ((uint32_t)vslot << 21));
+            st->move_log[3 * moves + 2] = (int)b;
+        }
+        ++moves;
+        cur ^= 1u;
+        if (moves >= max_moves) limit = true;
+        if (!grid_barrier(cs, nblocks, st, &ok_s)) {
+            timeout = true;
+            break;
+        }
+        if (limit) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long made = moves - moves0;
+        st->moves = moves;
+        st->total_moves += made;
+        st->sweeps += made + (limit || timeout || bad || start_done ? 0 : 1);
+        st->nbr_sweeps += sweeps;
+        st->cur = cur;
+        st->best_key = kNoMove;
+        for (int v = 0; v < kOrSlots; ++v) st->or_key[v] = kNoMove;
+        st->converged = 1;
+        if (limit) atomicOr(&st->status, kErrMoveLimit);
+        if (bad) atomicOr(&st->status, kErrBadKey);
+    }
+}
+
 __global__ void barrier_probe_kernel(CoopSync* cs, DevState* st) {
     __shared__ bool ok;
     grid_barrier(cs, 2u, st, &ok);
@@ -407,6 +558,34 @@ cudaError_t launch_coop_descent(const CoopArgs& A, int grid, cudaStream_t s) {
 cudaError_t launch_coop_ils(const CoopArgs& A, int grid, cudaStream_t s) {
     return A.n <= kCoopSmallN ? launch_coop_t<2, 32, 256, true>(A, grid, s)
                               : launch_coop_t<2, 32, 512, true>(A, grid, s);
+}
+
+template <bool OR, int NT>
+static int coop_nbr_grid_t(int device) {
+    int per_sm = 0, sms = 0, coop = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_nbr_kernel<OR, NT>, NT, 0) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess)
+        return 0;
+    if (!coop || per_sm < 1) return 0;
+    return per_sm * sms;
+}
+
+int coop_nbr_grid(uint32_t n, bool oropt, int device) {
+    const int nt = oropt ? 128 : 256;
+    const int cap = oropt ? coop_nbr_grid_t<true, 128>(device) : coop_nbr_grid_t<false, 256>(device);
+    const int want = (int)((n + nt - 1) / nt);
+    return cap < 1 ? 0 : (want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
+cudaError_t launch_coop_nbr(const NbrLaunch& L, CoopSync* cs, int grid, cudaStream_t s) {
+    void* args[] = {(void*)&L, (void*)&cs};
+    if (L.oropt)
+        return cudaLaunchCooperativeKernel((const void*)coop_nbr_kernel<true, 128>, grid, 128,
+                                           args, 0, s);
+    return cudaLaunchCooperativeKernel((const void*)coop_nbr_kernel<false, 256>, grid, 256, args,
+                                       0, s);
 }
 
 }  // namespace logo

@@ -89,12 +89,18 @@ cudaError_t launch_sweep_prepare(const SweepLaunch& L);
 bool sweep_shape_supported(int R, int NW, int variant);
 size_t sweep_smem_bytes(uint32_t cb);
 
+struct CoopSync;  // coop.cu's grid barrier and key slots (below)
+
 // ---- neighbour-list search (neighbour.cu) ------------------------------------
 struct NbrLaunch {
     const OrderedCity* Q0;
     const OrderedCity* Q1;
     const uint32_t* R0;
     const uint32_t* R1;
+    OrderedCity* Q0w;     // the same buffers, writable (the cooperative phase moves the tour)
+    OrderedCity* Q1w;
+    uint32_t* R0w;
+    uint32_t* R1w;
     uint32_t* pos;        // tour position of every city (exact: kept by every tour move)
     const uint32_t* nbr;  // K nearest other cities per city, nearest first
     uint32_t K;
@@ -110,6 +116,12 @@ constexpr uint32_t kSearchNeighbours = 8, kSearchNeighboursMax = 16;
 cudaError_t launch_nbr_sweep(const NbrLaunch& L, cudaStream_t s);
 // Recomputes pos from the current tour.
 cudaError_t launch_fill_pos(const NbrLaunch& L, cudaStream_t s);
+// The whole neighbour phase of a descent as one cooperative launch
+// (coop.cu): moves until no candidate improves or st->max_moves; cs must
+// hold count = gen = 0 and every slot = kNoMove.  coop_nbr_grid: its CTAs
+// for this n (0: cooperative launches unavailable).
+int coop_nbr_grid(uint32_t n, bool oropt, int device);
+cudaError_t launch_coop_nbr(const NbrLaunch& L, CoopSync* cs, int grid, cudaStream_t s);
 
 // ---- tour maintenance (tour.cu) --------------------------------------------
 struct TourBufs {
@@ -132,6 +144,7 @@ struct CoopSync {
     unsigned int count;            // CTAs arrived at the current barrier
     unsigned int gen;              // barrier generation
     unsigned long long slot[3];    // best key of move m in slot m % 3
+    unsigned long long or_slot[3][5];  // neighbour phase: Or-opt keys per variant
 };
 struct CoopArgs {
     OrderedCity* Q0;

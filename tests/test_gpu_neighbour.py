@@ -140,3 +140,24 @@ def test_tiny_tours_in_both_neighbour_modes(lg, inst, oracle_mod):
                     gils, gst = s.ils(r, 5, 3, lg.KICK_DOUBLE_BRIDGE)
                 assert np.array_equal(got, want) and st["moves"] == m, (n, oropt)
                 assert np.array_equal(gils, wils) and gst["final_length"] == wst["best_length"]
+
+
+@pytest.mark.parametrize("n,oropt", [(700, False), (9000, False), (30000, False), (4000, True),
+                                     (20000, True)])
+def test_cooperative_and_graph_neighbour_phase_agree(lg, inst, n, oropt):
+    """The neighbour phase as one cooperative launch (the default) and as
+    graph launches (LOGO_DESCENT_GRAPH) give the same tour, moves and
+    statistics."""
+    xy, r = _case(lg, inst, "clustered", n, 50 + n)
+    runs = []
+    for mode in (lg.DESCENT_AUTO, lg.DESCENT_GRAPH):
+        with lg.Solver(xy) as s:
+            s.set_search(lg.SEARCH_NEIGHBOUR_OROPT if oropt else lg.SEARCH_NEIGHBOUR)
+            s.set_descent_mode(mode)
+            got, st = s.optimize(r)
+            limited, st2 = s.optimize(r, max_moves=37)
+        runs.append((got, st["moves"], st["sweeps"], st["pair_evals"], st["final_length"],
+                     limited, st2["moves"]))
+    a, b = runs
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[5], b[5])
+    assert a[1:5] == b[1:5] and a[6] == b[6] == 37

@@ -5,11 +5,13 @@
 // gather from buffer cur into buffer cur^1 followed by a flip of cur made by
 // the last CTA to finish (threadfence + counter, no spinning), so the host
 // never touches the tour between moves.  Where the context keeps city
-// positions (the boxed sweep's seed pass), every kernel that moves the tour
-// writes them too; a position left stale (the cooperative descent does not
-// write them) only weakens the seed, never a result, because the seed pass
-// evaluates whatever pair of positions it reads exactly.
-//   init_ordered_kernel    ≙ ordered-coordinate gather, CUDASolver.cpp:316-319
+// positions (the boxed sweep's seed pass, the neighbour search), every
+// kernel that moves the tour writes them too; a position left stale (the
+// cooperative exhaustive descent does not write them) only weakens the
+// seed, never a result, because the seed pass evaluates whatever pair of
+// positions it reads exactly, and the neighbour search recomputes them
+// before its first use.
+//   load_route_kernel      ≙ ordered-coordinate gather, CUDASolver.cpp:316-319
 //   apply_move_kernel      ≙ rotate + reverse, twoOptLocalSolver.cpp:41-48
 //   tour_length_kernel     ≙ routeLength, headers.h:170-189
 //   kick_kernel            ≙ ILSGlobalSolver::kick, ILSGlobalSolver.cpp:37-48

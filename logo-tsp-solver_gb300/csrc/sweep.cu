@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(256)
                        const uint32_t* __restrict__ pos, const uint32_t* __restrict__ nbr,
                        uint32_t n, float4* __restrict__ wbox, float* __restrict__ wmax,
                        float4* __restrict__ rbox, float* __restrict__ rmax,
-                       uint32_t* __restrict__ workctl, DevState* st) {
+                       uint32_t* __restrict__ workctl, uint32_t stride, DevState* st) {
     chain_wait();
     chain_release();
     if (*(volatile unsigned int*)&st->converged) return;
@@ -384,9 +384,10 @@ __global__ void __launch_bounds__(256)
             rmax[g] = m;
         }
     }
-    // the seed: positions 3 + 32 g + lane, and 0, 1, 2 in the first warp
+    // the seed: positions 3 + stride * (32 g + lane), and 0, 1, 2 in the
+    // first warp
     uint64_t best = kNoMove;
-    const uint32_t i = 3 + g * kWin6 + lane;
+    const uint32_t i = 3 + stride * (g * kWin6 + lane);
     if (i < n) seed_position(Q, R, pos, nbr, n, i, best);
     if (g == 0 && lane < 3 && lane < n) seed_position(Q, R, pos, nbr, n, lane, best);
     best = warp_min_u64(best);
@@ -411,6 +412,16 @@ __global__ void __launch_bounds__(256)
 // n = 100k sweep of the benchmark's states 0.0645 ms with 4, 0.0688 with 1,
 // 0.0655 with 8; n = 1M random tour 0.208 ms with 8, 0.232 with 4).
 __host__ __device__ constexpr uint32_t filter_steps(uint32_t n) { return n >= 300000 ? 8u : 4u; }
+
+// Positions the seed pass evaluates: every one, or every stride-th on the
+// largest tours, where the pass is most of a sweep and a bound from a
+// sample of the positions prunes about as well.
+#ifndef LOGO_SEED_SPARSE
+#define LOGO_SEED_SPARSE 4
+#endif
+__host__ __device__ constexpr uint32_t seed_stride(uint32_t n) {
+    return n >= 500000 ? (uint32_t)LOGO_SEED_SPARSE : 1u;
+}
 
 // Tiles the filter lists first: those whose rows and columns are close
 // along the tour (the tile meets its row block's own positions), which on
@@ -814,7 +825,8 @@ static cudaError_t launch_boxed_t(const SweepLaunch& L, cudaStream_t s, bool pre
     const uint32_t grid = L.ntiles < resident ? L.ntiles : resident;
     const uint32_t nwin = max(sweep_windows(L.n), sweep_row_windows(L.n));
     e = launch_chained(window_seed_kernel, (nwin + 7) / 8, 256, 0, s, L.Q0, L.Q1, L.R0, L.R1,
-                       L.pos, L.nbr, L.n, L.wbox, L.wmax, L.rbox, L.rmax, L.workctl, L.st);
+                       L.pos, L.nbr, L.n, L.wbox, L.wmax, L.rbox, L.rmax, L.workctl,
+                       seed_stride(L.n), L.st);
     if (e != cudaSuccess) return e;
     const uint32_t rows_per_tile = (uint32_t)(NW * 32 * R);
     const uint32_t row_blocks = (L.n - 4) / rows_per_tile + 1;  // row0 + 3 <= n

@@ -415,7 +415,9 @@ __host__ __device__ constexpr uint32_t filter_steps(uint32_t n) { return n >= 30
 
 // Positions the seed pass evaluates: every one, or every stride-th on the
 // largest tours, where the pass is most of a sweep and a bound from a
-// sample of the positions prunes about as well.
+// sample of the positions prunes about as well (measured on GB300, n = 1M
+// uniform random tour: stride 1, 2, 3, 4, 8 -> 0.203, 0.158, 0.134, 0.129,
+// 0.260 ms per sweep).
 #ifndef LOGO_SEED_SPARSE
 #define LOGO_SEED_SPARSE 4
 #endif

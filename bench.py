@@ -404,16 +404,23 @@ def run_ours(a, world, rank, local, dist):
         "wall_s_timed_region": round(t_wall, 3),
     }
 
+    def block(name, fn, *args):
+        # an extra block that fails is reported in the line, not fatal to it
+        try:
+            out[name] = fn(*args)
+        except Exception as e:  # noqa: BLE001
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0 and a.dense:
-        out["dense"] = run_dense(s, xy, route, sm_max, local)
+        block("dense", run_dense, s, xy, route, sm_max, local)
     if rank == 0 and a.sweep_sizes:
-        out["sweep_per_n"] = run_sweep_per_n(a, sm_max, local)
+        block("sweep_per_n", run_sweep_per_n, a, sm_max, local)
     if rank == 0 and a.large_kicks:
-        out["large"] = run_large(a, local)
+        block("large", run_large, a, local)
     if a.batched and rank == 0:
-        out["batched"] = run_batched(a, local)
+        block("batched", run_batched, a, local)
     if a.serve_seconds > 0 and rank == 0:
-        out["serving"] = run_serving(a, local)
+        block("serving", run_serving, a, local)
 
     # CPU baseline: the oracle's multi-threaded sweep on this host (rank 0)
     if rank == 0 and a.cpu_sweeps > 0:

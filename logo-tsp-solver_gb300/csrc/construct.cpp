@@ -21,6 +21,7 @@
 #include <cstring>
 #include <queue>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/logo_gpu.h"
@@ -308,9 +309,12 @@ void knn_grid(const logo_xy* p, uint32_t n, uint32_t k, uint32_t* out) {
         std::vector<uint32_t> fill(start.begin(), start.end() - 1);
         for (uint32_t v = 0; v < n; ++v) items[fill[cellof[v]]++] = v;
     }
+    // every city's list depends on the grid alone: cities are split into
+    // contiguous ranges over host threads, the lists the same for any split
+    auto lists = [&](uint32_t v_lo, uint32_t v_hi) {
     std::vector<std::pair<double, uint32_t>> best;
     best.reserve(k + 1);
-    for (uint32_t v = 0; v < n; ++v) {
+    for (uint32_t v = v_lo; v < v_hi; ++v) {
         const double px = p[v].x, py = p[v].y;
         const int cx = (int)cx_of(px), cy = (int)cy_of(py);
         best.clear();
@@ -343,6 +347,16 @@ void knn_grid(const logo_xy* p, uint32_t n, uint32_t k, uint32_t* out) {
         for (uint32_t j = 0; j < k; ++j)
             out[(size_t)v * k + j] = best.empty() ? v : best[std::min<size_t>(j, best.size() - 1)].second;
     }
+    };
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = nt < 1 ? 1 : (nt > 16 ? 16 : nt);
+    if (n < 20000) nt = 1;  // not worth the threads
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t)
+        pool.emplace_back(lists, (uint32_t)((uint64_t)n * t / nt),
+                          (uint32_t)((uint64_t)n * (t + 1) / nt));
+    lists(0, (uint32_t)((uint64_t)n / nt));
+    for (auto& th : pool) th.join();
 }
 
 }  // namespace logo

@@ -28,6 +28,15 @@ def test_library_lists_equal_the_oracle(lg, inst, oracle_mod, k):
         assert np.array_equal(lg.neighbours(xy, k), oracle_mod.knn(xy, k)), (len(xy), k)
 
 
+def test_threaded_lists_equal_the_oracle(lg, inst, oracle_mod):
+    """From 20,000 cities the library splits the cities over host threads;
+    the lists must not depend on it."""
+    xy = inst.clustered(24000, 8, side=1.0e6, clusters=30)
+    assert np.array_equal(lg.neighbours(xy, 8), oracle_mod.knn(xy, 8))
+    xy = np.floor(inst.uniform_int(21000, 9) / 50.0).astype(np.float32)
+    assert np.array_equal(lg.neighbours(xy, 5), oracle_mod.knn(xy, 5))
+
+
 def test_small_and_longest_lists(lg, inst, oracle_mod):
     for n in range(1, 21):
         xy = inst.uniform_int(n, 100 + n)

@@ -152,6 +152,19 @@ private:
     uint32_t live_cells_;
 };
 
+// Host threads for the independent per-city queries of the start tour and
+// neighbour-list builders: none below 20,000 cities, else the machine's
+// (at most 16), or LOGO_HOST_THREADS when set.  Results do not depend on it.
+unsigned host_threads(uint32_t n) {
+    if (n < 20000) return 1;
+    if (const char* e = std::getenv("LOGO_HOST_THREADS")) {
+        const long v = std::strtol(e, nullptr, 10);
+        return v < 1 ? 1u : (v > 64 ? 64u : (unsigned)v);
+    }
+    const unsigned hw = std::thread::hardware_concurrency();
+    return hw < 1 ? 1u : (hw > 16 ? 16u : hw);
+}
+
 // nint(|a - b|) as an int: the per-edge distance in binary32 (this file is
 // compiled without FMA contraction), truncated like the reference's
 // fragment.distance (src/defs.h:201-205, from calculateDistance2D,
@@ -192,9 +205,23 @@ void mf_tour(const logo_xy* p, uint32_t n, uint32_t* route) {
     std::vector<uint32_t> link(n), tail(n);
     std::vector<int64_t> first(n, -1), second(n, -1);  // neighbours in join order
     std::priority_queue<Fragment, std::vector<Fragment>, LaterFragment> pq;
+    // every city's first link is a query on the full grid, independent of
+    // the others: split over host threads (the queue is then filled in
+    // city order, as before)
+    {
+        auto links = [&](uint32_t lo, uint32_t hi) {
+            for (uint32_t i = lo; i < hi; ++i) link[i] = grid.nearest(p[i].x, p[i].y, i);
+        };
+        const unsigned nt = host_threads(n);
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t)
+            pool.emplace_back(links, (uint32_t)((uint64_t)n * t / nt),
+                              (uint32_t)((uint64_t)n * (t + 1) / nt));
+        links(0, (uint32_t)((uint64_t)n / nt));
+        for (auto& th : pool) th.join();
+    }
     for (uint32_t i = 0; i < n; ++i) {
         tail[i] = i;
-        link[i] = grid.nearest(p[i].x, p[i].y, i);
         pq.push(Fragment{nint_dist(p[i], p[link[i]]), i});
     }
     for (uint32_t e = 0; e + 1 < n; ++e) {
@@ -348,9 +375,7 @@ void knn_grid(const logo_xy* p, uint32_t n, uint32_t k, uint32_t* out) {
             out[(size_t)v * k + j] = best.empty() ? v : best[std::min<size_t>(j, best.size() - 1)].second;
     }
     };
-    unsigned nt = std::thread::hardware_concurrency();
-    nt = nt < 1 ? 1 : (nt > 16 ? 16 : nt);
-    if (n < 20000) nt = 1;  // not worth the threads
+    const unsigned nt = host_threads(n);
     std::vector<std::thread> pool;
     for (unsigned t = 1; t < nt; ++t)
         pool.emplace_back(lists, (uint32_t)((uint64_t)n * t / nt),

@@ -105,3 +105,19 @@ def test_oropt_search_ends_at_a_local_optimum(inst, oracle_mod):
         assert oracle_mod.best_move(xy, got) == (0, 0, 0)
         assert 0 < nm <= m
         assert oracle_mod.tour_length(xy, got) < oracle_mod.tour_length(xy, plain)
+
+
+def test_host_builders_do_not_depend_on_the_thread_count(lg, inst, monkeypatch):
+    """The multiple-fragment tour and the neighbour lists split their
+    per-city queries over host threads from 20,000 cities; one thread gives
+    the same result."""
+    xy = inst.clustered(30000, 11, side=1.0e6, clusters=60)
+    dup = np.floor(inst.uniform_int(22000, 12) / 40.0).astype(np.float32)
+    many = (lg.mf_tour(xy), lg.mf_tour(dup), lg.neighbours(xy, 8), lg.neighbours(dup, 6))
+    monkeypatch.setenv("LOGO_HOST_THREADS", "1")
+    one = (lg.mf_tour(xy), lg.mf_tour(dup), lg.neighbours(xy, 8), lg.neighbours(dup, 6))
+    monkeypatch.setenv("LOGO_HOST_THREADS", "3")
+    three = (lg.mf_tour(xy), lg.mf_tour(dup), lg.neighbours(xy, 8), lg.neighbours(dup, 6))
+    for a, b, c in zip(many, one, three):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
+    assert lg.check_tour(many[0]) and lg.check_tour(many[1])

@@ -421,7 +421,9 @@ logo_status logo_mf_tour(const logo_xy *coords, uint32_t n, uint32_t *route);
  * nearest first, by squared distance in double with ties to the lower id;
  * with fewer than k other cities the remaining slots repeat the last one
  * found (v itself when n == 1).  The candidate lists of LOGO_SEARCH_NEIGHBOUR
- * (no reference counterpart). */
+ * (no reference counterpart).  From 20,000 cities this and logo_mf_tour
+ * spread their per-city queries over up to 16 host threads (the environment
+ * variable LOGO_HOST_THREADS sets the count); results do not depend on it. */
 logo_status logo_neighbours(const logo_xy *coords, uint32_t n, uint32_t k, uint32_t *out);
 
 /* Seeded random start tour (routeInit with ROUTE_INIT_SHUFFLE,

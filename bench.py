@@ -282,12 +282,20 @@ def barrier(dist):
 
 
 def reduce_max(dist, v):
+    """The largest v over the ranks (every rank gets it)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_rate(world, pairs, steps, seconds):
+    """Whole-job throughput: every rank decides `pairs` pairs per step for
+    `steps` steps (weak scaling), over the slowest rank's time."""
+    return world * pairs * steps / seconds
 
 
 def run_ours(a, world, rank, local, dist):
@@ -343,7 +351,7 @@ def run_ours(a, world, rank, local, dist):
     if converged or moves != a.warmup + 2 * a.steps:
         raise RuntimeError(f"descent ended early ({moves} moves); pick fewer steps")
     total_s = reduce_max(dist, sum(step_ms) / 1e3)
-    value = world * pairs * a.steps / total_s
+    value = job_rate(world, pairs, a.steps, total_s)
     ms_per_step = total_s * 1e3 / a.steps
 
     # e2e: the C-ABI call with host buffers, one move per call
@@ -357,7 +365,7 @@ def run_ours(a, world, rank, local, dist):
     for _ in range(a.e2e_steps):
         s.optimize_inplace(cur, max_moves=1)  # the caller's buffer, in and out
     e2e_s = reduce_max(dist, time.perf_counter() - t0)
-    e2e = {"value": world * pairs * a.e2e_steps / e2e_s, "unit": UNIT,
+    e2e = {"value": job_rate(world, pairs, a.e2e_steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n + 2 * 128,
            "call": "logo_descend(max_moves=1) per step on the caller's host buffer: "
                    "route in, sweep, argmin, reversal, route out (read and written in "

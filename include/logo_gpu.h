@@ -518,6 +518,13 @@ logo_status logo_ctx_set_route_io(logo_ctx *ctx, int mode);
  *   lower (segment start, gap).
  * neighbours: 1..16, 0 = 8.  INVALID_ARG for an unknown mode or list
  * length. */
+/* The start tour of the context's instance built on the device, written to
+ * route (n entries): LOGO_START_NN (equal to logo_nn_tour from city 0) or
+ * LOGO_START_MF (equal to logo_mf_tour), by one CTA as in the batched launch;
+ * n <= LOGO_BATCH_MAX_N, else INVALID_ARG (the host builders then).  The
+ * resident tour is not changed. */
+logo_status logo_start_tour(logo_ctx *ctx, int kind, uint32_t *route);
+
 #define LOGO_SEARCH_EXHAUSTIVE 0
 #define LOGO_SEARCH_NEIGHBOUR 1
 #define LOGO_SEARCH_NEIGHBOUR_OROPT 2

@@ -518,6 +518,21 @@ size_t mf_smem_bytes(uint32_t max_n) {
     return ((13 * (size_t)max_n + 15) & ~(size_t)15) + 4 * (size_t)max_n;
 }
 
+// A start tour of one instance (logo_start_tour on a single-instance
+// context): one CTA runs the batched launch's device builders (route
+// written to global memory).
+__global__ void __launch_bounds__(kMfThreads)
+    start_tour_kernel(const float2* __restrict__ xy, uint32_t n, int kind, uint32_t* route) {
+    extern __shared__ __align__(16) unsigned char st_smem[];
+    if (kind == kStartNN) {
+        nn_tour_cta<kMfThreads>(xy, n, route, reinterpret_cast<uint32_t*>(st_smem));
+    } else {
+        uint32_t* bbuf =
+            reinterpret_cast<uint32_t*>(st_smem + ((13 * (size_t)n + 15) & ~(size_t)15));
+        mf_tour_cta<kMfThreads>(xy, n, route, st_smem, bbuf);
+    }
+}
+
 template <int R, int NT, int TC>
 __global__ void __launch_bounds__(NT)
     batch_kernel(BatchArgs A) {
@@ -715,6 +730,19 @@ cudaError_t launch_mf_start(const float2* coords, uint32_t* routes, const BatchI
     const uint32_t grid = std::min<uint32_t>(count, (uint32_t)(sms > 0 ? sms : 1) * 4u);
     mf_start_kernel<<<grid, kMfThreads, mf_smem_bytes(max_n), s>>>(coords, routes, inst, order,
                                                                   count, max_n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_start_tour(const float2* xy, uint32_t n, int kind, uint32_t* route,
+                              cudaStream_t s) {
+    if (n == 0 || n > kBatchMaxN || (kind != kStartNN && kind != kStartMF))
+        return cudaErrorInvalidValue;
+    const size_t cap = std::max<size_t>(mf_smem_bytes(kBatchMaxN), sizeof(uint32_t) * kBatchMaxN);
+    cudaError_t e = cudaFuncSetAttribute(start_tour_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+    if (e != cudaSuccess) return e;
+    const size_t smem = kind == kStartNN ? sizeof(uint32_t) * n : mf_smem_bytes(n);
+    start_tour_kernel<<<1, kMfThreads, smem, s>>>(xy, n, kind, route);
     return cudaGetLastError();
 }
 

@@ -73,6 +73,10 @@ size_t batch_smem_bytes(uint32_t max_n);
 // prepare_mf_start (outside any stream capture) raises the kernel's shared
 // memory limit first.
 cudaError_t prepare_mf_start();
+// One instance's nearest-neighbour (kStartNN) or multiple-fragment
+// (kStartMF) start tour into route (device memory), n <= kBatchMaxN.
+cudaError_t launch_start_tour(const float2* xy, uint32_t n, int kind, uint32_t* route,
+                              cudaStream_t s);
 cudaError_t launch_mf_start(const float2* coords, uint32_t* routes, const BatchInstance* inst,
                             const uint32_t* order, uint32_t count, uint32_t max_n, int sms,
                             cudaStream_t s);

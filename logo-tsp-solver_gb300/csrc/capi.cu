@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/logo_gpu.h"
+#include "batch_internal.h"
 #include "logo_device.cuh"
 #include "logo_internal.h"
 
@@ -43,6 +44,7 @@ struct logo_ctx {
     cudaGraphExec_t nbr_chunk_exec = nullptr;  // nbr_chunk_steps x (neighbour sweep, apply)
     uint32_t nbr_chunk_steps = 32;
     int nbr_coop_grid = 0;        // CTAs of the cooperative neighbour phase (0: graphs)
+    uint32_t* d_start = nullptr;  // logo_start_tour's device output
     bool pageable_ok = false;     // the device reads and writes pageable host memory
     float4* d_wbox = nullptr;     // per-window boxes and largest edges (boxed sweep)
     float* d_wmax = nullptr;
@@ -772,6 +774,7 @@ void destroy(logo_ctx* c) {
     cudaFree(c->d_pos);
     cudaFree(c->d_nbr);
     cudaFree(c->d_nbr_search);
+    cudaFree(c->d_start);
     if (c->nbr_chunk_exec) cudaGraphExecDestroy(c->nbr_chunk_exec);
     cudaFree(c->d_coop);
     if (c->h_st) cudaFreeHost(c->h_st);
@@ -945,6 +948,27 @@ logo_status logo_ctx_get_info(const logo_ctx* c, logo_ctx_info* info) {
     info->search = c->search;
     info->search_neighbours = c->search_k;
     info->pad0 = 0;
+    return LOGO_OK;
+}
+
+logo_status logo_start_tour(logo_ctx* c, int kind, uint32_t* route) {
+    if (!c || !route) return LOGO_ERR_INVALID_ARG;
+    if (c->poisoned) return poisoned_error(c);
+    if (kind != LOGO_START_NN && kind != LOGO_START_MF)
+        return fail(c, LOGO_ERR_INVALID_ARG, "unknown start-tour kind");
+    if (c->n > LOGO_BATCH_MAX_N)
+        return fail(c, LOGO_ERR_INVALID_ARG,
+                    "device start tours hold the instance in one CTA (up to " +
+                        std::to_string(LOGO_BATCH_MAX_N) +
+                        " cities); larger tours: logo_nn_tour / logo_mf_tour");
+    CK(c, cudaSetDevice(c->device));
+    if (!c->d_start) CK(c, cudaMalloc(&c->d_start, sizeof(uint32_t) * c->n));
+    CK(c, launch_start_tour(c->d_xy, c->n, kind == LOGO_START_NN ? kStartNN : kStartMF,
+                            c->d_start, c->stream));
+    CK(c, cudaMemcpyAsync(route, c->d_start, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToHost,
+                          c->stream));
+    ++c->host_waits;
+    CK(c, cudaStreamSynchronize(c->stream));
     return LOGO_OK;
 }
 

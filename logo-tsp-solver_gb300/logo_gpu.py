@@ -58,7 +58,7 @@ EXPORTS = [
     "logo_server_create", "logo_server_submit", "logo_server_poll", "logo_server_wait",
     "logo_server_get_stats", "logo_server_destroy", "logo_server_last_error",
     "logo_diag_flag_timeout", "logo_ctx_set_route_io", "logo_ctx_set_search",
-    "logo_neighbours",
+    "logo_neighbours", "logo_start_tour",
 ]
 
 
@@ -185,6 +185,7 @@ def load(path=LIB_PATH):
     L.logo_ctx_set_descent_mode.argtypes = [_vp, c.c_int]
     L.logo_ctx_set_route_io.argtypes = [_vp, c.c_int]
     L.logo_ctx_set_search.argtypes = [_vp, c.c_int, c.c_uint32]
+    L.logo_start_tour.argtypes = [_vp, c.c_int, _u32p]
     L.logo_ctx_stream.restype = _vp
     L.logo_ctx_stream.argtypes = [_vp]
     L.logo_descend_trace.argtypes = [_vp, _u32p, c.c_uint64, ctypes.POINTER(ctypes.c_int32),
@@ -399,6 +400,13 @@ class Solver:
         """ROUTE_IO_AUTO, ROUTE_IO_COPY or ROUTE_IO_DIRECT (how route buffers
         reach the device; info()["route_io"] gives the mode in use)."""
         _check(load().logo_ctx_set_route_io(self._h, mode), self._h)
+
+    def start_tour(self, kind=START_NN):
+        """The instance's START_NN or START_MF tour built on the device
+        (n <= 4096)."""
+        r = np.zeros(self.n, dtype=np.uint32)
+        _check(load().logo_start_tour(self._h, kind, r.ctypes.data_as(_u32p)), self._h)
+        return r
 
     def set_search(self, mode, neighbours=0):
         """SEARCH_EXHAUSTIVE (the reference's best improvement) or

@@ -214,3 +214,17 @@ def test_batch_mf_start_built_on_device(lg, inst, kicks):
                 want, st = sol.optimize(mf)
             assert r["best_length"] == st["final_length"]
         assert np.array_equal(g, want), len(xy)
+
+
+def test_single_instance_start_tours_built_on_the_device(lg, inst):
+    """logo_start_tour: a single-instance context's NN and MF start tours
+    built by one CTA, equal to the host builders (ties and duplicate points
+    included); above the one-CTA limit the call is refused."""
+    for k, n in enumerate([3, 4, 5, 64, 1000, 2500, 4096]):
+        for xy in (inst.uniform_f32(n, 60 + k, 1.0e4),
+                   np.floor(inst.uniform_int(n, 70 + k) / 50.0).astype(np.float32)):
+            with lg.Solver(xy) as s:
+                assert np.array_equal(s.start_tour(lg.START_NN), lg.nn_tour(xy, 0)), n
+                assert np.array_equal(s.start_tour(lg.START_MF), lg.mf_tour(xy)), n
+    with lg.Solver(inst.uniform_f32(5000, 1, 1.0e4)) as s, pytest.raises(lg.LogoError):
+        s.start_tour(lg.START_NN)

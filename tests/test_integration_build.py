@@ -7,8 +7,10 @@
   liblogo_gpu.so.  Needs the reference checkout (REF, default
   /root/reference); skipped without it.
 * tests/c/abi_smoke.c, a plain C program that calls create, best move,
-  descend, tour length, ILS and destroy through include/logo_gpu.h: compiled
-  here with -Wall -Werror, and run on a GPU against the oracle.
+  descend, tour length, ILS, the device start tours, the neighbour-list
+  search, the copied route transfer and destroy through include/logo_gpu.h:
+  compiled here with -Wall -Werror, and run on a GPU against the oracle and
+  the host builders.
 """
 import os
 import shutil
@@ -88,3 +90,9 @@ def test_c_abi_smoke_program_matches_the_oracle(lg, inst, oracle_mod, tmp_path):
     best, st = oracle_mod.ils(xy, r, 10, 99, oracle_mod.KICK_DOUBLE_BRIDGE)
     assert rows["ils"][:3] == [st["best_length"], st["moves"], st["accepted"]]
     assert np.array_equal(np.array(rows["ils"][3:], dtype=np.uint32), best)
+    assert np.array_equal(np.array(rows["nnstart"], dtype=np.uint32), lg.nn_tour(xy, 0))
+    assert np.array_equal(np.array(rows["mfstart"], dtype=np.uint32), lg.mf_tour(xy))
+    nb, nm, _ = oracle_mod.descend_nbr(xy, r, k=8)
+    assert rows["nbrdescend"][0] == nm
+    assert np.array_equal(np.array(rows["nbrdescend"][2:], dtype=np.uint32), nb)
+    assert rows["copydescend"] == [m, oracle_mod.tour_length(xy, want)]

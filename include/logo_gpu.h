@@ -507,9 +507,9 @@ logo_status logo_ctx_set_route_io(logo_ctx *ctx, int mode);
  *   the whole pair set.  The end point is a 2-opt local optimum, reached
  *   along another path than the reference's, in far fewer pair evaluations
  *   at large n (no counterpart in the reference).  The neighbour phase of
- *   a descent is one cooperative launch where the device allows it (graph
- *   launches with LOGO_DESCENT_GRAPH, and inside logo_ils); the full sweeps
- *   after it use graph launches.
+ *   a descent is one cooperative launch where the device allows it (inside
+ *   logo_ils a cooperative kernel node of its graph; graph launches with
+ *   LOGO_DESCENT_GRAPH); the full sweeps after it use graph launches.
  * LOGO_SEARCH_NEIGHBOUR_OROPT: as NEIGHBOUR, and each step also weighs the
  *   Or-opt moves that create an edge to a listed neighbour: a segment of 1
  *   to 3 cities moved, in order or reversed, into another gap of the tour

@@ -441,7 +441,10 @@ cudaError_t capture_sweep_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
 cudaError_t capture_descent_loop(const logo_ctx* c, cudaStream_t s, cudaGraph_t g,
                                  cudaStream_t bs) {
     if (c->search == LOGO_SEARCH_EXHAUSTIVE) return capture_sweep_loop(c, s, g, bs, false);
-    cudaError_t e = capture_sweep_loop(c, s, g, bs, true);
+    // the neighbour phase: one cooperative kernel node where available
+    cudaError_t e = c->nbr_coop_grid > 0 && c->descent_mode != LOGO_DESCENT_GRAPH
+                        ? launch_coop_nbr(nbr_args(c), c->d_coop, c->nbr_coop_grid, s)
+                        : capture_sweep_loop(c, s, g, bs, true);
     if (e == cudaSuccess) e = launch_resume_descent(bufs(c), s);
     if (e == cudaSuccess) e = capture_sweep_loop(c, s, g, bs, false);
     return e;
@@ -1342,8 +1345,18 @@ logo_status logo_ils(logo_ctx* c, uint32_t* route, uint32_t kicks, uint64_t seed
         s = read_state(c);
     } else {
         // one graph: descent and kick loops are WHILE nodes on device conditions
-        CK(c, cudaGraphLaunch(c->ils_exec, c->stream));
-        s = read_state(c);
+        const bool nbr_coop = c->search != LOGO_SEARCH_EXHAUSTIVE && c->nbr_coop_grid > 0 &&
+                              c->descent_mode != LOGO_DESCENT_GRAPH;
+        if (nbr_coop) {  // the neighbour phases are cooperative kernel nodes
+            CK(c, cudaMemsetAsync(c->d_coop, 0xFF, sizeof(CoopSync), c->stream));
+            CK(c, cudaMemsetAsync(c->d_coop, 0, 2 * sizeof(unsigned int), c->stream));
+            std::lock_guard<std::mutex> lk(coop_lock(c->device));
+            CK(c, cudaGraphLaunch(c->ils_exec, c->stream));
+            s = read_state(c);
+        } else {
+            CK(c, cudaGraphLaunch(c->ils_exec, c->stream));
+            s = read_state(c);
+        }
     }
     if (s != LOGO_OK) return s;
     const DevState fin = *c->h_st;

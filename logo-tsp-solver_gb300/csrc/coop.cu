@@ -505,6 +505,16 @@ __global__ void __launch_bounds__(NT) coop_nbr_kernel(NbrLaunch L, CoopSync* cs)
         }
         if (limit) break;
     }
+    // leave the key slots empty for the next launch (a graph replays this
+    // one without a memset in between): every CTA has read its last slot
+    // once all have passed one more barrier
+    if (!timeout && grid_barrier(cs, nblocks, st, &ok_s) && blockIdx.x == 0 &&
+        threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) {
+            cs->slot[k] = kNoMove;
+            for (int v = 0; v < kOrSlots; ++v) cs->or_slot[k][v] = kNoMove;
+        }
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long made = moves - moves0;
         st->moves = moves;
@@ -580,12 +590,20 @@ int coop_nbr_grid(uint32_t n, bool oropt, int device) {
 }
 
 cudaError_t launch_coop_nbr(const NbrLaunch& L, CoopSync* cs, int grid, cudaStream_t s) {
-    void* args[] = {(void*)&L, (void*)&cs};
-    if (L.oropt)
-        return cudaLaunchCooperativeKernel((const void*)coop_nbr_kernel<true, 128>, grid, 128,
-                                           args, 0, s);
-    return cudaLaunchCooperativeKernel((const void*)coop_nbr_kernel<false, 256>, grid, 256, args,
-                                       0, s);
+    // a cooperative launch through the launch attribute, which stream capture
+    // records as a cooperative kernel node (the device-run ILS graph)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(L.oropt ? 128u : 256u);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (L.oropt) return cudaLaunchKernelEx(&cfg, coop_nbr_kernel<true, 128>, L, cs);
+    return cudaLaunchKernelEx(&cfg, coop_nbr_kernel<false, 256>, L, cs);
 }
 
 }  // namespace logo
